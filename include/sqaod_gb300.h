@@ -1,0 +1,273 @@
+/*
+ * sqaod_gb300.h -- C ABI of the GB300-native sqaod annealing / brute-force
+ * search hot path (libsqaod_gb300.so).
+ *
+ * Two layers, both plain C (pointers, sizes, status codes; no C++ or torch
+ * types):
+ *
+ *  1. Solver-handle layer (sq103_dg_annealer_*, sq103_bg_annealer_*,
+ *     sq103_dg_bf_*, sq103_bg_bf_*).  One entry point per method of the
+ *     reference's CPython method tables, so a binding (ctypes, cffi, a CPython
+ *     extension) maps one-to-one onto them:
+ *       annealers:     sqaodc/pyglue/annealer.inc:885-908
+ *       BF searchers:  sqaodc/pyglue/bf_searcher.inc:479-494
+ *     behind which stand the C++ interfaces sqaod::cuda::DenseGraphAnnealer,
+ *     BipartiteGraphAnnealer, DenseGraphBFSearcher, BipartiteGraphBFSearcher
+ *     <float> (sqaodc/cuda/api.h:40-67, sqaodc/common/Solver.h:17-252); the
+ *     same classes are exported as C++ through include/sqaodc/.
+ *
+ *  2. Kernel layer (sq103_dense_*, sq103_bipartite_*, sq103_bf_*): device
+ *     pointers, a caller-supplied stream (void * = cudaStream_t), no
+ *     allocation.  These replace the reference's device math
+ *     (sqaodc/cuda/DeviceFormulas.cpp, DeviceMath.cpp, DeviceKernels.cu,
+ *     DeviceDenseGraphBatchSearch.cu, DeviceBipartiteGraphBatchSearch.cu) and
+ *     the per-step sweeps of CUDADenseGraphAnnealer.cu / CUDABipartiteGraphAnnealer.cu.
+ *
+ * Every function returns 0 on success.  Handle-layer functions return -1 on a
+ * user error (the reference throws std::runtime_error there,
+ * sqaodc/common/defines.h:43-46) with the message available from
+ * sq103_last_error(); positive values are CUDA error codes or sq103 device
+ * status codes (1 = a bounded device wait timed out, 2 = bad shape,
+ * 3 = capacity exceeded).
+ *
+ * Layouts: matrices are row-major and dense (row stride = number of columns
+ * unless an ld argument says otherwise); spins q are int8 {-1, +1}; bits x are
+ * int8 {0, 1}; packed bit sets put variable i at bit (N - 1 - i) (MSB-first,
+ * sqaodc/common/Common.cpp:79-93).  optimize: 0 = minimise, 1 = maximise
+ * (sqaodc/common/Solver.h:10-15).
+ */
+#ifndef SQAOD_GB300_H
+#define SQAOD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SQ103_API __attribute__((visibility("default")))
+#else
+#define SQ103_API
+#endif
+
+/* ------------------------------------------------------------ common */
+
+/* message of the last failed handle-layer call on this thread */
+SQ103_API const char *sq103_last_error(void);
+/* library version (1.0.3 of the reference API: sqaodc/common/defines.h:80) */
+SQ103_API int sq103_version(void);
+
+/* ------------------------------------------------ kernel layer: dense */
+
+/* One dense annealing instance for the sweep kernels.  Replaces the state
+ * the reference keeps in CUDADenseGraphAnnealer (sqaodc/cuda/CUDADenseGraphAnnealer.h). */
+typedef struct sq103_dense_task {
+    const float *J;       /* N x N Ising couplings, row stride ldJ, zero diagonal, symmetric */
+    const float *h;       /* N */
+    int8_t *q;            /* m x N spins, row stride N */
+    float *F;             /* m x N local fields F[y][i] = sum_j J[i][j] q[y][j] */
+    uint32_t *trace;      /* optional: accept bits per step (layout in the design doc) */
+    unsigned long long *accepted; /* optional: accepted-flip counter (atomically added) */
+    const float *G;       /* nSteps transverse fields (kT for SA), device memory; or NULL: use Gs */
+    const float *beta;    /* nSteps inverse temperatures (ignored by SA); or NULL: use betas */
+    float Gs, betas;      /* G and beta of every step when the arrays are NULL */
+    int *status;          /* optional device status word (timeouts) */
+    uint64_t seed;        /* Philox key */
+    uint32_t step0;       /* Philox step counter of the first step */
+    int N, m, ldJ;
+    int algo;             /* 0 naive, 1 coloring, 2 sa_naive */
+    int nSteps;
+} sq103_dense_task;
+
+/* QUBO -> Ising (h, J, c); replaces DeviceDenseGraphFormulas::calculateHamiltonian
+ * (sqaodc/cuda/DeviceFormulas.cpp:24-31).  scratch: N doubles. */
+SQ103_API int sq103_dense_hamiltonian(const float *W, int ldW, int N, int maximize, float *h, float *J,
+                                      int ldJ, float *c, double *c64, double *scratch, void *stream);
+/* F = q J for all trotters (the local-field refresh). */
+SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q, float *F, int N, int m,
+                                        void *stream);
+/* FP64 Ising energies of all trotters (calculate_E; sqaodc/cuda/DeviceFormulas.cpp:42-49).
+ * r_scratch: m x N doubles. */
+SQ103_API int sq103_dense_energy(const float *J, int ldJ, const float *h, const double *c64,
+                                 const int8_t *q, int N, int m, int maximize, double *r_scratch,
+                                 double *E64, float *E32, void *stream);
+/* sum_y q_y . q_{y+1} (DeviceDotSpins, sqaodc/cuda/DeviceBatchedDot.cuh:145-160) */
+SQ103_API int sq103_ring_dot(const int8_t *q, int N, int m, long long *out, void *stream);
+/* randomizeSpin (sqaodc/cuda/DeviceKernels.cu:550-572) from the Philox stream */
+SQ103_API int sq103_randomize_spins(int8_t *q, int N, int m, uint64_t seed, uint32_t step, int tagSide,
+                                    void *stream);
+/* nSteps annealOneStep sweeps of one instance (CUDADenseGraphAnnealer::annealOneStepSQA/SA,
+ * sqaodc/cuda/CUDADenseGraphAnnealer.cu:524-602).  The task is passed by value. */
+SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream);
+/* nTasks instances in one launch; d_tasks lives in device memory. */
+SQ103_API int sq103_dense_anneal_batch(const sq103_dense_task *d_tasks, int nTasks, int maxN, int maxM,
+                                       void *stream);
+
+/* -------------------------------------------- kernel layer: bipartite */
+
+typedef struct sq103_bipartite_task {
+    const float *J;       /* N1 x N0 */
+    const float *h0, *h1; /* N0, N1 */
+    int8_t *q0, *q1;      /* m x N0, m x N1 */
+    float *F0, *F1;       /* m x N0, m x N1 field scratch */
+    uint32_t *trace;
+    unsigned long long *accepted;
+    const float *G, *beta; /* device arrays of nSteps entries, or NULL: use Gs / betas */
+    float Gs, betas;
+    uint64_t seed;
+    uint32_t step0;
+    int N0, N1, m, algo, nSteps;
+} sq103_bipartite_task;
+
+/* (sqaodc/cuda/DeviceFormulas.cpp:107-117). scratch: N0 + N1 doubles */
+SQ103_API int sq103_bipartite_hamiltonian(const float *b0, const float *b1, const float *W, int N0,
+                                          int N1, int maximize, float *h0, float *h1, float *J, float *c,
+                                          double *c64, double *scratch, void *stream);
+/* side 1: F[y][i] = sum_j J[i][j] qFixed[y][j];  side 0: F[y][j] = sum_i qFixed[y][i] J[i][j]
+ * (the per-half-step cuBLAS GEMMs of CUDABipartiteGraphAnnealer.cu:393-401) */
+SQ103_API int sq103_bipartite_fields(const float *J, int N0, int N1, const int8_t *qFixed, int side,
+                                     float *F, int m, void *stream);
+/* FP64 energies (sqaodc/cuda/DeviceFormulas.cpp:120-140); r_scratch: m x N1 doubles */
+SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const float *h1, const double *c64,
+                                     const int8_t *q0, const int8_t *q1, int N0, int N1, int m,
+                                     int maximize, double *r_scratch, double *E64, float *E32,
+                                     void *stream);
+/* nSteps annealOneStep of one bipartite instance
+ * (CUDABipartiteGraphAnnealer::annealOneStepSQA/SA, :539-625) */
+SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task, void *stream);
+
+/* ------------------------------------------------- kernel layer: BF */
+
+/* Dense BF over [xBegin, xEnd): fp32 energies of x^T W x (W already signed
+ * for the optimisation direction), then every x with E <= Emin + slack is
+ * written to cand (up to cap; *count gets the true number).
+ * ws: workspace of sq103_bf_workspace_bytes(N) bytes.
+ * Replaces DeviceDenseGraphBatchSearch::{calculate_E, partition_xMins, select}
+ * (sqaodc/cuda/DeviceDenseGraphBatchSearch.cu:58-187). */
+SQ103_API size_t sq103_bf_workspace_bytes(int N);
+SQ103_API int sq103_dense_bf_range(const float *W, int N, uint64_t xBegin, uint64_t xEnd, float slack,
+                                   void *ws, uint64_t *cand, int cap, int *count, float *Emin32,
+                                   void *stream);
+/* FP64 energies of packed states (tie-break of the candidates) */
+SQ103_API int sq103_dense_bf_refine(const float *W, int N, const uint64_t *x, int n, double *E,
+                                    void *stream);
+/* Bipartite BF over [x0b, x0e) x [x1b, x1e) (DeviceBipartiteGraphBatchSearch.cu:65-217).
+ * cand receives (x0, x1) pairs. ws: sq103_bf_workspace_bytes(N0 + N1) bytes. */
+SQ103_API int sq103_bipartite_bf_range(const float *b0, const float *b1, const float *W, int N0, int N1,
+                                       uint64_t x0b, uint64_t x0e, uint64_t x1b, uint64_t x1e,
+                                       float slack, void *ws, uint64_t *cand, int cap, int *count,
+                                       float *Emin32, void *stream);
+SQ103_API int sq103_bipartite_bf_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
+                                        const uint64_t *pairs, int n, double *E, void *stream);
+
+/* ------------------------------------------- handle layer: annealers */
+/* Mirrors annealer.inc:885-908.  Preferences are passed as strings, as the
+ * reference parses them (sqaodc/common/Preference.cpp:61-78):
+ * algorithm = naive|coloring|sa_naive|sa_coloring|default|sa_default,
+ * n_trotters = <int>.  sq103_*_get_preferences writes
+ * "algorithm=...;n_trotters=...;precision=float;device=cuda". */
+
+SQ103_API int sq103_dg_annealer_new(void **handle);
+SQ103_API int sq103_dg_annealer_delete(void *handle);
+SQ103_API int sq103_dg_annealer_seed(void *handle, unsigned long long seed);
+SQ103_API int sq103_dg_annealer_set_qubo(void *handle, const float *W, int N, int optimize);
+SQ103_API int sq103_dg_annealer_set_hamiltonian(void *handle, const float *h, const float *J, float c,
+                                                int N);
+SQ103_API int sq103_dg_annealer_get_problem_size(void *handle, int *N);
+SQ103_API int sq103_dg_annealer_set_preference(void *handle, const char *name, const char *value);
+SQ103_API int sq103_dg_annealer_get_preferences(void *handle, char *buf, int buflen);
+SQ103_API int sq103_dg_annealer_get_E(void *handle, float *E, int cap, int *n);
+SQ103_API int sq103_dg_annealer_get_x(void *handle, int8_t *x, int capRows, int *m);
+SQ103_API int sq103_dg_annealer_get_hamiltonian(void *handle, float *h, float *J, float *c);
+SQ103_API int sq103_dg_annealer_get_q(void *handle, int8_t *q, int capRows, int *m);
+SQ103_API int sq103_dg_annealer_set_q(void *handle, const int8_t *q, int N);
+SQ103_API int sq103_dg_annealer_set_qset(void *handle, const int8_t *q, int m, int N);
+SQ103_API int sq103_dg_annealer_randomize_spin(void *handle);
+SQ103_API int sq103_dg_annealer_calculate_E(void *handle);
+SQ103_API int sq103_dg_annealer_prepare(void *handle);
+SQ103_API int sq103_dg_annealer_make_solution(void *handle);
+SQ103_API int sq103_dg_annealer_get_system_E(void *handle, float G, float beta, float *E);
+SQ103_API int sq103_dg_annealer_anneal_one_step(void *handle, float G, float beta);
+/* initAnneal: prepare() + randomizeSpin() (named by the target API; the
+ * reference has no such method) */
+SQ103_API int sq103_dg_annealer_init_anneal(void *handle);
+/* extensions: a whole schedule in one call; FP64 energies; counters; trace */
+SQ103_API int sq103_dg_annealer_anneal(void *handle, const float *G, const float *beta, int nSteps);
+SQ103_API int sq103_dg_annealer_get_E64(void *handle, double *E, int cap, int *n);
+SQ103_API int sq103_dg_annealer_get_accepted(void *handle, unsigned long long *accepted);
+SQ103_API int sq103_dg_annealer_get_rng_state(void *handle, unsigned long long *seed, uint32_t *step);
+SQ103_API int sq103_dg_annealer_set_trace(void *handle, int enable);
+SQ103_API int sq103_dg_annealer_get_trace(void *handle, uint32_t *bits, int nwords);
+
+SQ103_API int sq103_bg_annealer_new(void **handle);
+SQ103_API int sq103_bg_annealer_delete(void *handle);
+SQ103_API int sq103_bg_annealer_seed(void *handle, unsigned long long seed);
+SQ103_API int sq103_bg_annealer_set_qubo(void *handle, const float *b0, const float *b1, const float *W,
+                                         int N0, int N1, int optimize);
+SQ103_API int sq103_bg_annealer_set_hamiltonian(void *handle, const float *h0, const float *h1,
+                                                const float *J, float c, int N0, int N1);
+SQ103_API int sq103_bg_annealer_get_problem_size(void *handle, int *N0, int *N1);
+SQ103_API int sq103_bg_annealer_set_preference(void *handle, const char *name, const char *value);
+SQ103_API int sq103_bg_annealer_get_preferences(void *handle, char *buf, int buflen);
+SQ103_API int sq103_bg_annealer_get_E(void *handle, float *E, int cap, int *n);
+SQ103_API int sq103_bg_annealer_get_x(void *handle, int8_t *x0, int8_t *x1, int capRows, int *m);
+SQ103_API int sq103_bg_annealer_get_hamiltonian(void *handle, float *h0, float *h1, float *J, float *c);
+SQ103_API int sq103_bg_annealer_get_q(void *handle, int8_t *q0, int8_t *q1, int capRows, int *m);
+SQ103_API int sq103_bg_annealer_set_q(void *handle, const int8_t *q0, const int8_t *q1, int N0, int N1);
+SQ103_API int sq103_bg_annealer_set_qset(void *handle, const int8_t *q0, const int8_t *q1, int m, int N0,
+                                         int N1);
+SQ103_API int sq103_bg_annealer_randomize_spin(void *handle);
+SQ103_API int sq103_bg_annealer_calculate_E(void *handle);
+SQ103_API int sq103_bg_annealer_prepare(void *handle);
+SQ103_API int sq103_bg_annealer_make_solution(void *handle);
+SQ103_API int sq103_bg_annealer_get_system_E(void *handle, float G, float beta, float *E);
+SQ103_API int sq103_bg_annealer_anneal_one_step(void *handle, float G, float beta);
+SQ103_API int sq103_bg_annealer_init_anneal(void *handle);
+SQ103_API int sq103_bg_annealer_anneal(void *handle, const float *G, const float *beta, int nSteps);
+SQ103_API int sq103_bg_annealer_get_E64(void *handle, double *E, int cap, int *n);
+SQ103_API int sq103_bg_annealer_get_accepted(void *handle, unsigned long long *accepted);
+SQ103_API int sq103_bg_annealer_get_rng_state(void *handle, unsigned long long *seed, uint32_t *step);
+SQ103_API int sq103_bg_annealer_set_trace(void *handle, int enable);
+SQ103_API int sq103_bg_annealer_get_trace(void *handle, uint32_t *bits, int nwords);
+
+/* ---------------------------------------- handle layer: BF searchers */
+/* Mirrors bf_searcher.inc:479-494.  Preferences: tile_size (dense),
+ * tile_size_0 / tile_size_1 (bipartite). */
+
+SQ103_API int sq103_dg_bf_new(void **handle);
+SQ103_API int sq103_dg_bf_delete(void *handle);
+SQ103_API int sq103_dg_bf_set_qubo(void *handle, const float *W, int N, int optimize);
+SQ103_API int sq103_dg_bf_get_problem_size(void *handle, int *N);
+SQ103_API int sq103_dg_bf_set_preference(void *handle, const char *name, const char *value);
+SQ103_API int sq103_dg_bf_get_preferences(void *handle, char *buf, int buflen);
+SQ103_API int sq103_dg_bf_get_x(void *handle, int8_t *x, int capRows, int *n);
+SQ103_API int sq103_dg_bf_get_E(void *handle, float *E, int cap, int *n);
+SQ103_API int sq103_dg_bf_prepare(void *handle);
+SQ103_API int sq103_dg_bf_calculate_E(void *handle);
+SQ103_API int sq103_dg_bf_make_solution(void *handle);
+/* one tile; *done = 1 when the whole range is searched; curXEnd may be NULL */
+SQ103_API int sq103_dg_bf_search_range(void *handle, unsigned long long *curXEnd, int *done);
+SQ103_API int sq103_dg_bf_search(void *handle);
+
+SQ103_API int sq103_bg_bf_new(void **handle);
+SQ103_API int sq103_bg_bf_delete(void *handle);
+SQ103_API int sq103_bg_bf_set_qubo(void *handle, const float *b0, const float *b1, const float *W, int N0,
+                                   int N1, int optimize);
+SQ103_API int sq103_bg_bf_get_problem_size(void *handle, int *N0, int *N1);
+SQ103_API int sq103_bg_bf_set_preference(void *handle, const char *name, const char *value);
+SQ103_API int sq103_bg_bf_get_preferences(void *handle, char *buf, int buflen);
+SQ103_API int sq103_bg_bf_get_x(void *handle, int8_t *x0, int8_t *x1, int capRows, int *n);
+SQ103_API int sq103_bg_bf_get_E(void *handle, float *E, int cap, int *n);
+SQ103_API int sq103_bg_bf_prepare(void *handle);
+SQ103_API int sq103_bg_bf_calculate_E(void *handle);
+SQ103_API int sq103_bg_bf_make_solution(void *handle);
+SQ103_API int sq103_bg_bf_search_range(void *handle, unsigned long long *curX0, unsigned long long *curX1,
+                                       int *done);
+SQ103_API int sq103_bg_bf_search(void *handle);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SQAOD_GB300_H */

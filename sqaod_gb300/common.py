@@ -1,0 +1,172 @@
+"""Python-side helpers of the sqaod API (sqaodpy/sqaod/common/{common,preference}.py):
+algorithm names, optimisation direction tags, input checks and conversions,
+random problem generators and the anneal() loop."""
+import numbers
+import sys
+
+import numpy as np
+
+
+class Algorithm:
+    default = 'default'
+    naive = 'naive'
+    coloring = 'coloring'
+    brute_force_search = 'brute_force_search'
+    sa_default = 'sa_default'
+    sa_naive = 'sa_naive'
+    sa_coloring = 'sa_coloring'
+
+    @staticmethod
+    def is_sqa(algo):
+        return algo in (Algorithm.default, Algorithm.naive, Algorithm.coloring)
+
+
+algorithm = Algorithm()
+
+
+class Minimize:
+    """Tag for minimisation."""
+
+    @staticmethod
+    def sign(v):
+        return v.copy()
+
+    @staticmethod
+    def best(values):
+        return min(values)
+
+    @staticmethod
+    def sort(values):
+        return sorted(values)
+
+    def __int__(self):
+        return 0
+
+
+class Maximize:
+    """Tag for maximisation."""
+
+    @staticmethod
+    def sign(v):
+        return -v
+
+    @staticmethod
+    def best(values):
+        return max(values)
+
+    @staticmethod
+    def sort(values):
+        return sorted(values, reverse=True)
+
+    def __int__(self):
+        return 1
+
+
+minimize = Minimize()
+maximize = Maximize()
+
+# tolerances of the symmetry check (sqaodpy/sqaod/common/common.py:8-11)
+rtol_fp64, atol_fp64 = 1.0e-5, 1.0e-8
+rtol_fp32, atol_fp32 = 1.0e-4, 1.0e-5
+
+
+def optimize_flag(optimize):
+    if optimize is maximize or isinstance(optimize, Maximize):
+        return 1
+    if optimize is minimize or isinstance(optimize, Minimize):
+        return 0
+    if optimize in (0, 1):
+        return int(optimize)
+    raise ValueError("optimize must be sqaod_gb300.minimize or sqaod_gb300.maximize")
+
+
+def is_symmetric(mat):
+    rtol, atol = (rtol_fp64, atol_fp64) if mat.dtype == np.float64 else (rtol_fp32, atol_fp32)
+    return np.allclose(mat, mat.T, rtol, atol)
+
+
+def is_triangular(mat):
+    atol = rtol_fp64 if mat.dtype == np.float64 else rtol_fp32
+    if not np.any(np.triu(mat, 1) > atol):
+        return True
+    return not np.any(np.tril(mat, -1) > atol)
+
+
+def symmetrize(mat):
+    """Symmetric input is returned as is; a triangular one becomes (W + W^T) / 2."""
+    if is_symmetric(mat):
+        return mat
+    if is_triangular(mat):
+        return (mat + mat.T) * 0.5
+    raise RuntimeError("given matrix is not triangular nor symmetric.")
+
+
+def fix_type(obj, dtype):
+    if isinstance(obj, np.ndarray):
+        if obj.dtype == dtype and obj.flags['C_CONTIGUOUS']:
+            return obj
+        return np.asarray(obj, dtype=dtype, order='C')
+    return [fix_type(np.asarray(o), dtype) for o in obj]
+
+
+def check_square(W, name='W'):
+    if not isinstance(W, np.ndarray) or W.ndim != 2 or W.shape[0] != W.shape[1]:
+        raise RuntimeError('%s should be a square matrix.' % name)
+
+
+def generate_random_symmetric_W(N, wmin=-0.5, wmax=0.5, dtype=np.float64):
+    """Upper triangle iid uniform in [wmin, wmax), mirrored
+    (sqaodpy/sqaod/common/common.py:70-78, same draws from np.random)."""
+    W = np.zeros((N, N), dtype)
+    for i in range(N):
+        for j in range(i, N):
+            W[i, j] = np.random.random()
+    W = W + np.tril(np.ones((N, N)), -1) * W.T
+    return W * (wmax - wmin) + wmin
+
+
+def create_bitset_sequence(vals, nbits):
+    vals = np.asarray(list(vals), dtype=np.uint64)
+    shifts = np.arange(nbits - 1, -1, -1, dtype=np.uint64)
+    return ((vals[:, None] >> shifts[None, :]) & np.uint64(1)).astype(np.int8)
+
+
+def randomize_spin(qmat):
+    qmat[...] = np.random.choice([-1, 1], qmat.shape).astype(qmat.dtype)
+
+
+def bit_to_spin(x):
+    return x * 2 - 1
+
+
+def bit_from_spin(q):
+    return (q + 1) >> 1
+
+
+def anneal(annealer, Ginit=5., Gfin=0.01, beta=1. / 0.02, tau=0.99, n_repeat=10, verbose=False):
+    """Repeats prepare / randomize_spin / geometric schedule / make_solution and
+    returns the best (E, x) found (sqaodpy/sqaod/common/common.py:144-160)."""
+    best_E = sys.float_info.max
+    best_x = None
+    opt = annealer.get_optimize_dir() if hasattr(annealer, 'get_optimize_dir') else minimize
+    sign = -1. if isinstance(opt, Maximize) else 1.
+    for _ in range(n_repeat):
+        annealer.prepare()
+        annealer.randomize_spin()
+        G = Ginit
+        while Gfin < G:
+            annealer.anneal_one_step(G, beta)
+            if verbose:
+                annealer.calculate_E()
+                print(annealer.get_E())
+            G *= tau
+        annealer.make_solution()
+        E = np.asarray(annealer.get_E())
+        i = int(np.argmin(sign * E))
+        if sign * E[i] < sign * best_E or best_x is None:
+            best_E, best_x = E[i], annealer.get_x()[i]
+    return best_E, best_x
+
+
+def is_scalar(v):
+    return isinstance(v, numbers.Number)

@@ -1,0 +1,315 @@
+// bf.cu -- brute-force QUBO search (dense and bipartite graphs).
+//
+// Dense: E(x) = x^T W x over packed states x (variable i at bit N-1-i,
+// sqaodc/common/Common.cpp:79-93).  A state splits into hi = x >> L (the
+// first N-L variables) and lo = x & (2^L - 1) (the last L variables,
+// L = min(N, 14)):
+//   E = E_hh(hi) + E_ll(lo) + sum_{b in lo} x_b C_hi[b],   C_hi[b] = 2 sum_{i in hi} W_{i,b}
+// One CTA per hi value; E_ll is a 2^L table shared by all CTAs and the cross
+// term is two table lookups over the halves of lo.  The search runs in three
+// passes: fp32 minimum, collection of every x with E32 <= Emin32 + slack, and
+// an FP64 re-evaluation of the candidates (tie-break) done by the caller
+// through sq103_dense_bf_refine.  For integer-valued W every fp32 value is
+// exact, so Emin and the argmin set equal the reference CPU searcher's
+// (sqaodc/cpu/CPUDenseGraphBatchSearch.cpp:26-50).
+//
+// Bipartite: E(x0, x1) = b0.x0 + b1.x1 + x1^T W x0 (sqaodc/cpu/SharedFormulas.cpp:123-144).
+// One CTA per x1 value; D[j] = b0[j] + sum_{i in x1} W[i][j]; E is the sum of
+// 7-bit-group lookups over x0 plus b1.x1.
+#include <cstring>
+
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+constexpr int kLoBits = 14;
+constexpr int kBfThreads = 256;
+
+struct BfWorkspace {
+    float ell[1 << kLoBits];
+    unsigned int minEnc;
+    int count;
+    int pad[62];
+};
+
+__device__ __forceinline__ unsigned int enc_float(float f) {
+    unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float dec_float(unsigned int e) {
+    unsigned int u = (e & 0x80000000u) ? (e & 0x7fffffffu) : ~e;
+    return __uint_as_float(u);
+}
+
+__global__ void bf_init_ws(BfWorkspace *ws) {
+    ws->minEnc = 0xffffffffu;
+    ws->count = 0;
+}
+
+// E_ll table: lo bit b <-> variable N-1-b
+__global__ void bf_lo_table(const float *W, int N, int L, BfWorkspace *ws) {
+    int lo = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lo >= (1 << L)) return;
+    double e = 0.;
+    for (int a = 0; a < L; ++a) {
+        if (!((lo >> a) & 1)) continue;
+        int va = N - 1 - a;
+        for (int b = 0; b < L; ++b)
+            if ((lo >> b) & 1) e += (double)W[(size_t)va * N + (N - 1 - b)];
+    }
+    ws->ell[lo] = (float)e;
+}
+
+// per-CTA setup for one hi value: base = E_hh(hi); tabHi / tabLo = cross term halves
+__device__ void bf_block_setup(const float *W, int N, int L, uint64_t hi, float *base, float *tabHi,
+                               float *tabLo, float *C, int Lh, int Ll) {
+    int H = N - L;
+    int tid = threadIdx.x;
+    // C[b] = 2 sum_{i in hi set} W[i][N-1-b]; hi bit c <-> variable H-1-c
+    if (tid < L) {
+        double s = 0.;
+        for (int c = 0; c < H; ++c)
+            if ((hi >> c) & 1ull) s += (double)W[(size_t)(H - 1 - c) * N + (N - 1 - tid)];
+        C[tid] = (float)(2. * s);
+    }
+    if (tid == 32) {
+        double e = 0.;
+        for (int c = 0; c < H; ++c) {
+            if (!((hi >> c) & 1ull)) continue;
+            const float *row = W + (size_t)(H - 1 - c) * N;
+            for (int d = 0; d < H; ++d)
+                if ((hi >> d) & 1ull) e += (double)row[H - 1 - d];
+        }
+        *base = (float)e;
+    }
+    __syncthreads();
+    // tables over the two halves of lo: lo = (a << Ll) | b
+    for (int t = tid; t < (1 << Lh); t += blockDim.x) {
+        float s = 0.f;
+        for (int k = 0; k < Lh; ++k)
+            if ((t >> k) & 1) s += C[Ll + k];
+        tabHi[t] = s;
+    }
+    for (int t = tid; t < (1 << Ll); t += blockDim.x) {
+        float s = 0.f;
+        for (int k = 0; k < Ll; ++k)
+            if ((t >> k) & 1) s += C[k];
+        tabLo[t] = s;
+    }
+    __syncthreads();
+}
+
+// PASS 0: minimum; PASS 1: collect x with E <= thr
+template <int PASS>
+__global__ void __launch_bounds__(kBfThreads) bf_dense_pass(const float *W, int N, int L, uint64_t xb, uint64_t xe,
+                                                            float slack, BfWorkspace *ws, uint64_t *cand, int cap) {
+    __shared__ float tabHi[128], tabLo[128], C[kLoBits];
+    __shared__ float base;
+    __shared__ unsigned int blockMin;
+    const int Lh = L / 2, Ll = L - Lh;
+    const uint64_t hb = xb >> L, he = (xe - 1) >> L;
+    float thr = 0.f;
+    if (PASS == 1) thr = dec_float(ws->minEnc) + slack;
+    for (uint64_t hi = hb + blockIdx.x; hi <= he; hi += gridDim.x) {
+        bf_block_setup(W, N, L, hi, &base, tabHi, tabLo, C, Lh, Ll);
+        if (PASS == 0 && threadIdx.x == 0) blockMin = 0xffffffffu;
+        __syncthreads();
+        uint64_t x0 = hi << L;
+        uint32_t loB = (uint32_t)(xb > x0 ? xb - x0 : 0);
+        uint32_t loE = (uint32_t)min((uint64_t)1 << L, xe - x0);
+        float lmin = __int_as_float(0x7f800000);
+        const uint32_t mask = (1u << Ll) - 1u;
+        for (uint32_t lo = loB + threadIdx.x; lo < loE; lo += blockDim.x) {
+            float e = (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]);
+            if (PASS == 0) {
+                lmin = fminf(lmin, e);
+            } else if (e <= thr) {
+                int slot = atomicAdd(&ws->count, 1);
+                if (slot < cap) cand[slot] = x0 | lo;
+            }
+        }
+        if (PASS == 0) {
+            for (int o = 16; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+            if ((threadIdx.x & 31) == 0) atomicMin(&blockMin, enc_float(lmin));
+            __syncthreads();
+            if (threadIdx.x == 0) atomicMin(&ws->minEnc, blockMin);
+        }
+        __syncthreads();
+    }
+}
+
+// bipartite: x1 per CTA; x0 through 7-bit-group tables
+template <int PASS>
+__global__ void __launch_bounds__(kBfThreads) bf_bip_pass(const float *b0, const float *b1, const float *W, int N0,
+                                                          int N1, uint64_t x0b, uint64_t x0e, uint64_t x1b,
+                                                          uint64_t x1e, float slack, BfWorkspace *ws,
+                                                          uint64_t *cand, int cap) {
+    __shared__ float tab[9][128];
+    __shared__ float D[64];
+    __shared__ float base;
+    __shared__ unsigned int blockMin;
+    const int nG = (N0 + 6) / 7;
+    float thr = 0.f;
+    if (PASS == 1) thr = dec_float(ws->minEnc) + slack;
+    for (uint64_t x1 = x1b + blockIdx.x; x1 < x1e; x1 += gridDim.x) {
+        int tid = threadIdx.x;
+        // x0 bit c <-> variable N0-1-c ; x1 bit c <-> variable N1-1-c
+        if (tid < N0) {
+            int j = N0 - 1 - tid;  // D indexed by x0 bit position
+            double s = (double)b0[j];
+            for (int c = 0; c < N1; ++c)
+                if ((x1 >> c) & 1ull) s += (double)W[(size_t)(N1 - 1 - c) * N0 + j];
+            D[tid] = (float)s;
+        }
+        if (tid == 64) {
+            double s = 0.;
+            for (int c = 0; c < N1; ++c)
+                if ((x1 >> c) & 1ull) s += (double)b1[N1 - 1 - c];
+            base = (float)s;
+        }
+        if (PASS == 0 && tid == 0) blockMin = 0xffffffffu;
+        __syncthreads();
+        for (int t = tid; t < nG * 128; t += blockDim.x) {
+            int g = t >> 7, v = t & 127;
+            float s = 0.f;
+            for (int k = 0; k < 7; ++k) {
+                int bit = g * 7 + k;
+                if (bit < N0 && ((v >> k) & 1)) s += D[bit];
+            }
+            tab[g][v] = s;
+        }
+        __syncthreads();
+        float lmin = __int_as_float(0x7f800000);
+        for (uint64_t x0 = x0b + tid; x0 < x0e; x0 += blockDim.x) {
+            float e = base;
+            for (int g = 0; g < nG; ++g) e += tab[g][(x0 >> (7 * g)) & 127];
+            if (PASS == 0) {
+                lmin = fminf(lmin, e);
+            } else if (e <= thr) {
+                int slot = atomicAdd(&ws->count, 1);
+                if (slot < cap) {
+                    cand[2 * slot] = x0;
+                    cand[2 * slot + 1] = x1;
+                }
+            }
+        }
+        if (PASS == 0) {
+            for (int o = 16; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+            if ((tid & 31) == 0) atomicMin(&blockMin, enc_float(lmin));
+            __syncthreads();
+            if (tid == 0) atomicMin(&ws->minEnc, blockMin);
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 energies of packed dense states, one warp per state
+__global__ void bf_dense_refine(const float *W, int N, const uint64_t *xs, int n, double *E) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    uint64_t x = xs[w];
+    double s = 0.;
+    for (int i = lane; i < N; i += 32) {
+        if (!((x >> (N - 1 - i)) & 1ull)) continue;
+        for (int j = 0; j < N; ++j)
+            if ((x >> (N - 1 - j)) & 1ull) s += (double)W[(size_t)i * N + j];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) E[w] = s;
+}
+
+__global__ void bf_bip_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
+                              const uint64_t *pairs, int n, double *E) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    uint64_t x0 = pairs[2 * w], x1 = pairs[2 * w + 1];
+    double s = 0.;
+    for (int j = lane; j < N0; j += 32)
+        if ((x0 >> (N0 - 1 - j)) & 1ull) s += (double)b0[j];
+    for (int i = lane; i < N1; i += 32) {
+        if (!((x1 >> (N1 - 1 - i)) & 1ull)) continue;
+        s += (double)b1[i];
+        for (int j = 0; j < N0; ++j)
+            if ((x0 >> (N0 - 1 - j)) & 1ull) s += (double)W[(size_t)i * N0 + j];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) E[w] = s;
+}
+
+static int bf_grid(uint64_t units) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t g = (uint64_t)sms * 8;
+    return (int)(units < g ? units : g);
+}
+
+}  // namespace sq103
+
+using namespace sq103;
+
+extern "C" {
+
+SQ103_API size_t sq103_bf_workspace_bytes(int N) {
+    (void)N;
+    return sizeof(BfWorkspace);
+}
+
+SQ103_API int sq103_dense_bf_range(const float *W, int N, uint64_t xBegin, uint64_t xEnd, float slack, void *ws,
+                                   uint64_t *cand, int cap, int *count, float *Emin32, void *stream) {
+    if (N <= 0 || N > 63 || xEnd <= xBegin || xEnd > (1ull << N)) return kErrBadShape;
+    cudaStream_t s = (cudaStream_t)stream;
+    BfWorkspace *w = (BfWorkspace *)ws;
+    int L = N < kLoBits ? N : kLoBits;
+    bf_init_ws<<<1, 1, 0, s>>>(w);
+    bf_lo_table<<<((1 << L) + 255) / 256, 256, 0, s>>>(W, N, L, w);
+    uint64_t nHi = ((xEnd - 1) >> L) - (xBegin >> L) + 1;
+    int grid = bf_grid(nHi);
+    bf_dense_pass<0><<<grid, kBfThreads, 0, s>>>(W, N, L, xBegin, xEnd, slack, w, cand, cap);
+    bf_dense_pass<1><<<grid, kBfThreads, 0, s>>>(W, N, L, xBegin, xEnd, slack, w, cand, cap);
+    unsigned int enc = 0;
+    cudaMemcpyAsync(count, &w->count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&enc, &w->minEnc, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int)e;
+    unsigned int u = (enc & 0x80000000u) ? (enc & 0x7fffffffu) : ~enc;
+    memcpy(Emin32, &u, sizeof(float));
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_bf_refine(const float *W, int N, const uint64_t *x, int n, double *E, void *stream) {
+    if (n <= 0) return 0;
+    bf_dense_refine<<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(W, N, x, n, E);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_bf_range(const float *b0, const float *b1, const float *W, int N0, int N1,
+                                       uint64_t x0b, uint64_t x0e, uint64_t x1b, uint64_t x1e, float slack,
+                                       void *ws, uint64_t *cand, int cap, int *count, float *Emin32,
+                                       void *stream) {
+    if (N0 <= 0 || N1 <= 0 || N0 > 63 || N1 > 63 || x0e <= x0b || x1e <= x1b) return kErrBadShape;
+    cudaStream_t s = (cudaStream_t)stream;
+    BfWorkspace *w = (BfWorkspace *)ws;
+    bf_init_ws<<<1, 1, 0, s>>>(w);
+    int grid = bf_grid(x1e - x1b);
+    bf_bip_pass<0><<<grid, kBfThreads, 0, s>>>(b0, b1, W, N0, N1, x0b, x0e, x1b, x1e, slack, w, cand, cap);
+    bf_bip_pass<1><<<grid, kBfThreads, 0, s>>>(b0, b1, W, N0, N1, x0b, x0e, x1b, x1e, slack, w, cand, cap);
+    unsigned int enc = 0;
+    cudaMemcpyAsync(count, &w->count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&enc, &w->minEnc, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int)e;
+    unsigned int u = (enc & 0x80000000u) ? (enc & 0x7fffffffu) : ~enc;
+    memcpy(Emin32, &u, sizeof(float));
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_bf_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
+                                        const uint64_t *pairs, int n, double *E, void *stream) {
+    if (n <= 0) return 0;
+    bf_bip_refine<<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(b0, b1, W, N0, N1, pairs, n, E);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

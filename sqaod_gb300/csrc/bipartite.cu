@@ -1,0 +1,196 @@
+// bipartite.cu -- bipartite-graph Suzuki-Trotter / SA sweeps.
+//
+// One annealOneStep = a half-step on side 1 followed by a half-step on side 0
+// (CUDABipartiteGraphAnnealer::annealOneStepSQA, sqaodc/cuda/CUDABipartiteGraphAnnealer.cu:539-560;
+// CPUBipartiteGraphAnnealer::annealOneStepColoringParallel, sqaodc/cpu/CPUBipartiteGraphAnnealer.cpp:434-441).
+// A half-step computes the fields of the moving side from the fixed side
+// (F1 = q0 J^T or F0 = q1 J, spin GEMM), then flips every spin of the moving
+// side in colour phases: even trotters, trotter m-1 when m is odd, odd
+// trotters.  Spin i of trotter y draws u from philox((i, y, step, 0x31 | side << 8)).w1:
+//   dE = (2/m) q (h + F) - q (q_{y-1} + q_{y+1}) coef  (SQA),  2 q (h + F)  (SA, 0x32).
+// Unlike the reference GPU kernel (which feeds trotters 2g and 2g+1 the same
+// uniform, CUDABipartiteGraphAnnealer.cu:486,499) every trial has its own draw.
+//
+// naive: (N0+N1) m sequential trials at (x, y) = (hi(w0 (N0+N1)), hi(w1 m)) of
+// philox((t, 0, step, 0x33)) (CPUBipartiteGraphAnnealer.cpp:290-328);
+// sa_naive: per trotter, (N0+N1) m trials at x = hi(w0 (N0+N1)) of
+// philox((t, y, step, 0x34)) (CPUBipartiteGraphAnnealer.cpp:446-480).
+// The naive fields are a fixed-order block reduction of one J row or column.
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+__global__ void __launch_bounds__(256) bip_flip_phase(int8_t *qA, const float *F, const float *h, int Ns, int m,
+                                                      int yb, int ys, int cnt, uint64_t seed, uint32_t step,
+                                                      uint32_t tag, const float *Gp, const float *bp, float Gsc, float bsc,
+                                                      int algo, uint32_t *trace, unsigned long long bitBase,
+                                                      unsigned long long *accepted) {
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = idx < (long long)cnt * Ns;
+    int acc = 0;
+    if (active) {
+        StepConst sc = step_const(algo, m, Gp ? *Gp : Gsc, bp ? *bp : bsc);
+        int t = (int)(idx / Ns), i = (int)(idx - (long long)t * Ns);
+        int y = yb + t * ys;
+        u32x4 r = draw(seed, (uint32_t)i, (uint32_t)y, step, tag);
+        float u = draw_unit(r.y);
+        size_t o = (size_t)y * Ns + i;
+        float qyx = qA[o];
+        float dE;
+        if (algo == kSAColoring) {
+            dE = bip_sa_dE(qyx, h[i], F[o]);
+        } else {
+            int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
+            dE = bip_sqa_dE(qyx, h[i], F[o], qA[(size_t)yl * Ns + i], qA[(size_t)yr * Ns + i], sc.twoDivM,
+                            sc.coef);
+        }
+        if (metropolis(dE, sc.rate, u)) {
+            qA[o] = (int8_t)(-qyx);
+            acc = 1;
+            if (trace) {
+                unsigned long long bit = bitBase + o;
+                atomicOr(&trace[bit >> 5], 1u << (bit & 31));
+            }
+        }
+    }
+    if (accepted) {
+        unsigned ballot = __ballot_sync(0xffffffffu, acc);
+        if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(accepted, (unsigned long long)__popc(ballot));
+    }
+}
+
+// fixed-order block sum (256 threads) in fp32
+__device__ float block_sum_f32(float v, float *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (warp == 0) {
+        r = lane < 8 ? red[lane] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    __syncthreads();
+    return r;
+}
+
+// field on spin x of `side` in trotter y (fixed-order reduction)
+__device__ float bip_field_at(const sq103_bipartite_task &T, int side, int y, int x, float *red) {
+    float s = 0.f;
+    if (side == 0) {
+        for (int i = threadIdx.x; i < T.N1; i += 256)
+            s = __fmaf_rn(T.J[(size_t)i * T.N0 + x], (float)T.q1[(size_t)y * T.N1 + i], s);
+    } else {
+        for (int j = threadIdx.x; j < T.N0; j += 256)
+            s = __fmaf_rn(T.J[(size_t)x * T.N0 + j], (float)T.q0[(size_t)y * T.N0 + j], s);
+    }
+    return block_sum_f32(s, red);
+}
+
+// naive (one CTA, grid 1) or sa_naive (one CTA per trotter)
+__global__ void __launch_bounds__(256) bip_naive(sq103_bipartite_task T, int s) {
+    __shared__ float red[8];
+    __shared__ int sx, sy, sside;
+    __shared__ float su;
+    const bool sa = T.algo == kSANaive;
+    const StepConst sc = step_const(T.algo, T.m, T.G ? T.G[s] : T.Gs, T.beta ? T.beta[s] : T.betas);
+    const uint32_t step = T.step0 + (uint32_t)s;
+    const int Ntot = T.N0 + T.N1;
+    const long long perY = (long long)Ntot * T.m;
+    const int yFixed = blockIdx.x;
+    unsigned long long accepted = 0;
+    for (long long t = 0; t < perY; ++t) {
+        if (threadIdx.x == 0) {
+            u32x4 r = draw(T.seed, (uint32_t)t, sa ? (uint32_t)yFixed : 0u, step, sa ? kTagBipSANaive : kTagBipNaive);
+            int x = draw_index(r.x, Ntot);
+            sy = sa ? yFixed : draw_index(r.y, T.m);
+            su = draw_unit(sa ? r.y : r.z);
+            sside = x < T.N0 ? 0 : 1;
+            sx = sside ? x - T.N0 : x;
+        }
+        __syncthreads();
+        int x = sx, y = sy, side = sside;
+        float F = bip_field_at(T, side, y, x, red);
+        if (threadIdx.x == 0) {
+            int Ns = side ? T.N1 : T.N0;
+            int8_t *qA = side ? T.q1 : T.q0;
+            const float *h = side ? T.h1 : T.h0;
+            float qyx = qA[(size_t)y * Ns + x];
+            float dE;
+            if (sa) {
+                dE = bip_sa_dE(qyx, h[x], F);
+            } else {
+                int yl = y == 0 ? T.m - 1 : y - 1, yr = y == T.m - 1 ? 0 : y + 1;
+                dE = bip_sqa_dE(qyx, h[x], F, qA[(size_t)yl * Ns + x], qA[(size_t)yr * Ns + x], sc.twoDivM,
+                                sc.coef);
+            }
+            if (metropolis(dE, sc.rate, su)) {
+                qA[(size_t)y * Ns + x] = (int8_t)(-qyx);
+                ++accepted;
+                if (T.trace) {
+                    unsigned long long bit = (sa ? (unsigned long long)yFixed * perY : 0ull) + (unsigned long long)t;
+                    uint32_t *tr = T.trace + (size_t)s * ((perY * (sa ? T.m : 1) + 31) / 32);
+                    atomicOr(&tr[bit >> 5], 1u << (bit & 31));
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && T.accepted) atomicAdd(T.accepted, accepted);
+}
+
+}  // namespace sq103
+
+using namespace sq103;
+
+extern "C" SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task, void *stream) {
+    if (!task) return kErrBadShape;
+    const sq103_bipartite_task &T = *task;
+    if (T.N0 <= 0 || T.N1 <= 0 || T.m <= 0) return kErrBadShape;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int m = T.m, m2 = (m / 2) * 2;
+    for (int s = 0; s < T.nSteps; ++s) {
+        const uint32_t step = T.step0 + (uint32_t)s;
+        if (T.algo == kNaive || T.algo == kSANaive) {
+            bip_naive<<<T.algo == kSANaive ? m : 1, 256, 0, st>>>(T, s);
+            continue;
+        }
+        const bool sa = T.algo == kSAColoring;
+        const unsigned long long wordsPerStep = ((unsigned long long)m * (T.N0 + T.N1) + 31) / 32;
+        uint32_t *trace = T.trace ? T.trace + (size_t)s * wordsPerStep : nullptr;
+        unsigned long long bitBase = 0;
+        for (int hs = 0; hs < 2; ++hs) {
+            const int side = hs == 0 ? 1 : 0;
+            const int Ns = side ? T.N1 : T.N0;
+            int8_t *qA = side ? T.q1 : T.q0;
+            float *F = side ? T.F1 : T.F0;
+            const float *h = side ? T.h1 : T.h0;
+            sq103_bipartite_fields(T.J, T.N0, T.N1, side ? T.q0 : T.q1, side, F, m, stream);
+            const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
+            for (int ph = 0; ph < 3; ++ph) {
+                int yb, ys, cnt;
+                if (sa) {
+                    if (ph) break;
+                    yb = 0; ys = 1; cnt = m;
+                } else if (ph == 0) {
+                    yb = 0; ys = 2; cnt = m2 / 2;
+                } else if (ph == 1) {
+                    if (!(m & 1)) continue;
+                    yb = m - 1; ys = 1; cnt = 1;
+                } else {
+                    yb = 1; ys = 2; cnt = m2 / 2;
+                }
+                if (cnt == 0) continue;
+                long long n = (long long)cnt * Ns;
+                bip_flip_phase<<<(int)((n + 255) / 256), 256, 0, st>>>(qA, F, h, Ns, m, yb, ys, cnt, T.seed, step, tag,
+                                                                       T.G ? T.G + s : nullptr,
+                                                                       T.beta ? T.beta + s : nullptr, T.Gs, T.betas,
+                                                                       T.algo, trace, bitBase,
+                                                                       T.accepted);
+            }
+            bitBase += (unsigned long long)m * Ns;
+        }
+    }
+    return (int)cudaGetLastError();
+}

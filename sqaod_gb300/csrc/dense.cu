@@ -1,0 +1,265 @@
+// dense.cu -- dense-graph Suzuki-Trotter / SA sweeps and spin randomisation.
+//
+// Algorithms (one annealOneStep; the FP64 host replay restates the same rules):
+//   coloring (SQA): for k in [0, N): phase A = even trotters y < 2*(m/2), phase
+//     B = trotter m-1 when m is odd, phase C = odd trotters.  In each phase every
+//     trotter makes one trial at x = hi(w0 * N) with u = (w1 >> 8) 2^-24 drawn
+//     from philox((k, y, step, 0x11)):
+//       dE = (2/m) q_yx (h_x + 2 F_yx) - q_yx (q_{y-1,x} + q_{y+1,x}) coef,
+//       coef = log(tanh(G beta / m)) / beta, accept iff dE < 0 or exp(-beta dE) > u.
+//     This is the colour order of CPUDenseGraphAnnealer::annealColoredPlaneParallel
+//     (sqaodc/cpu/CPUDenseGraphAnnealer.cpp:304-338) and of tryFlipSQAKernel
+//     (sqaodc/cuda/CUDADenseGraphAnnealer.cu:430-519).
+//   sa_naive: every trotter makes N trials (philox((k, y, step, 0x12))),
+//     dE = 2 q (h + 2 F), accept iff exp(-dE / G) > u
+//     (CPUDenseGraphAnnealer.cpp:342-371, CUDADenseGraphAnnealer.cu:545-602).
+//   naive: N m sequential trials at (y, x) = (hi(w0 m), hi(w1 N)) from
+//     philox((t, 0, step, 0x13)) (CPUDenseGraphAnnealer.cpp:268-279).
+//
+// Instead of the reference's per-trial row dot J[x] . q[y] (4N bytes of J per
+// trial), the kernels keep the local fields F[y][i] = sum_j J[i][j] q[y][j]
+// resident and apply a rank-1 update F[y][:] += -2 q_yx J[x][:] per accepted
+// flip (one J row streamed per accepted flip).  Updates of a row are applied
+// in trial order with one rounding each, so every kernel that runs the same
+// trials holds bit-identical fields.
+#include <cstdio>
+
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+struct Flip {
+    int y, x;
+    float d;
+};
+
+constexpr int kBlockThreads = 512;
+
+// Applies the flips of one phase: F[y_f][i] += d_f * J[x_f][i].
+__device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F, const float *J, int ldJ, int N) {
+    int tid = threadIdx.x;
+    if (N >= kBlockThreads || nf == 1) {
+        for (int f = 0; f < nf; ++f) {
+            Flip fl = flips[f];
+            float *Fy = F + (size_t)fl.y * N;
+            const float *Jx = J + (size_t)fl.x * ldJ;
+            for (int i = tid; i < N; i += kBlockThreads) Fy[i] = __fmaf_rn(fl.d, __ldg(Jx + i), Fy[i]);
+        }
+    } else {
+        int groups = kBlockThreads / N;
+        int g = tid / N, i = tid - g * N;
+        if (g < groups)
+            for (int f = g; f < nf; f += groups) {
+                Flip fl = flips[f];
+                F[(size_t)fl.y * N + i] = __fmaf_rn(fl.d, __ldg(J + (size_t)fl.x * ldJ + i), F[(size_t)fl.y * N + i]);
+            }
+    }
+}
+
+// One CTA anneals one instance (all trotters).  Spins, fields and h are staged
+// in shared memory when they fit; otherwise the CTA works on global memory.
+__global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_dense_task *tasks,
+                                                                 sq103_dense_task single, int smemBytes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const sq103_dense_task T = tasks ? tasks[blockIdx.x] : single;
+    const int N = T.N, m = T.m, tid = threadIdx.x;
+    Flip *flips = reinterpret_cast<Flip *>(smem);            // 2 x m
+    int *nflip = reinterpret_cast<int *>(flips + 2 * m);      // 2 counters
+    size_t off = ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
+    size_t stageBytes = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
+    const bool stage = off + stageBytes <= (size_t)smemBytes;
+    float *F;
+    const float *h;
+    int8_t *q;
+    if (stage) {
+        F = reinterpret_cast<float *>(smem + off);
+        float *hs = F + (size_t)m * N;
+        q = reinterpret_cast<int8_t *>(hs + N);
+        for (size_t i = tid; i < (size_t)m * N; i += kBlockThreads) {
+            F[i] = T.F[i];
+            q[i] = T.q[i];
+        }
+        for (int i = tid; i < N; i += kBlockThreads) hs[i] = T.h[i];
+        h = hs;
+    } else {
+        F = T.F;
+        h = T.h;
+        q = T.q;
+    }
+    if (tid < 2) nflip[tid] = 0;
+    __syncthreads();
+
+    const uint32_t wordsPerStep = (uint32_t)(((size_t)N * m + 31) / 32);
+    unsigned long long accepted = 0;
+    __shared__ Flip naiveFlip;
+    __shared__ int naiveAcc;
+
+    for (int s = 0; s < T.nSteps; ++s) {
+        const float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
+        const StepConst sc = step_const(T.algo, m, G, beta);
+        const uint32_t step = T.step0 + (uint32_t)s;
+        uint32_t *trace = T.trace ? T.trace + (size_t)s * wordsPerStep : nullptr;
+
+        if (T.algo == kNaive) {
+            const long long nTrials = (long long)N * m;
+            for (long long t = 0; t < nTrials; ++t) {
+                if (tid == 0) {
+                    u32x4 r = draw(T.seed, (uint32_t)t, 0u, step, kTagDenseNaive);
+                    int y = draw_index(r.x, m), x = draw_index(r.y, N);
+                    float u = draw_unit(r.z);
+                    size_t o = (size_t)y * N + x;
+                    float qyx = q[o];
+                    int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
+                    float dE = dense_sqa_dE(qyx, h[x], F[o], q[(size_t)yl * N + x], q[(size_t)yr * N + x],
+                                            sc.twoDivM, sc.coef);
+                    int acc = metropolis(dE, sc.rate, u);
+                    if (acc) {
+                        q[o] = (int8_t)(-qyx);
+                        naiveFlip = Flip{y, x, -2.f * qyx};
+                        if (trace) atomicOr(&trace[t >> 5], 1u << (t & 31));
+                        ++accepted;
+                    }
+                    naiveAcc = acc;
+                }
+                __syncthreads();
+                if (naiveAcc) apply_flips(&naiveFlip, 1, F, T.J, T.ldJ, N);
+                __syncthreads();
+            }
+            continue;
+        }
+
+        const bool sa = (T.algo == kSANaive);
+        const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
+        int buf = 0;
+        for (int k = 0; k < N; ++k) {
+            for (int ph = 0; ph < 3; ++ph) {
+                int yb, ys, cnt;
+                if (sa) {
+                    if (ph) break;
+                    yb = 0; ys = 1; cnt = m;
+                } else if (ph == 0) {
+                    yb = 0; ys = 2; cnt = m / 2;
+                } else if (ph == 1) {
+                    if (!(m & 1)) continue;
+                    yb = m - 1; ys = 1; cnt = 1;
+                } else {
+                    yb = 1; ys = 2; cnt = m / 2;
+                }
+                Flip *fl = flips + buf * m;
+                for (int t = tid; t < cnt; t += kBlockThreads) {
+                    int y = yb + t * ys;
+                    u32x4 r = draw(T.seed, (uint32_t)k, (uint32_t)y, step, tag);
+                    int x = draw_index(r.x, N);
+                    float u = draw_unit(r.y);
+                    size_t o = (size_t)y * N + x;
+                    float qyx = q[o];
+                    float dE;
+                    if (sa) {
+                        dE = dense_sa_dE(qyx, h[x], F[o]);
+                    } else {
+                        int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
+                        dE = dense_sqa_dE(qyx, h[x], F[o], q[(size_t)yl * N + x], q[(size_t)yr * N + x],
+                                          sc.twoDivM, sc.coef);
+                    }
+                    if (metropolis(dE, sc.rate, u)) {
+                        q[o] = (int8_t)(-qyx);
+                        int slot = atomicAdd(&nflip[buf], 1);
+                        fl[slot] = Flip{y, x, -2.f * qyx};
+                        if (trace) {
+                            uint32_t bit = (uint32_t)k * (uint32_t)m + (uint32_t)y;
+                            atomicOr(&trace[bit >> 5], 1u << (bit & 31));
+                        }
+                    }
+                }
+                __syncthreads();
+                int nf = nflip[buf];
+                apply_flips(fl, nf, F, T.J, T.ldJ, N);
+                if (tid == 0) {
+                    nflip[buf ^ 1] = 0;
+                    accepted += (unsigned long long)nf;
+                }
+                __syncthreads();
+                buf ^= 1;
+            }
+        }
+    }
+
+    if (tid == 0 && T.accepted) atomicAdd(T.accepted, accepted);
+    if (stage) {
+        for (size_t i = tid; i < (size_t)m * N; i += kBlockThreads) {
+            T.F[i] = F[i];
+            T.q[i] = q[i];
+        }
+    }
+}
+
+__global__ void randomize_kernel(int8_t *q, int N, int m, uint64_t seed, uint32_t step, uint32_t tag) {
+    int chunks = (N + 127) / 128;
+    long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)m * chunks) return;
+    int y = (int)(idx / chunks), c = (int)(idx - (long long)y * chunks);
+    u32x4 r = draw(seed, (uint32_t)c, (uint32_t)y, step, tag);
+    uint32_t w[4] = {r.x, r.y, r.z, r.w};
+    int8_t *qy = q + (size_t)y * N + (size_t)c * 128;
+    int nb = min(128, N - c * 128);
+    for (int b = 0; b < nb; ++b) qy[b] = ((w[b >> 5] >> (b & 31)) & 1u) ? 1 : -1;
+}
+
+static int g_max_smem = -1;
+
+static int max_dyn_smem() {
+    if (g_max_smem < 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        g_max_smem = v;
+        cudaFuncSetAttribute(dense_sweep_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+    }
+    return g_max_smem;
+}
+
+static size_t cta_smem_bytes(int N, int m) {
+    size_t base = ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
+    size_t stage = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
+    size_t lim = (size_t)max_dyn_smem() - 1024;  // static shared memory headroom
+    if (base + stage <= lim) return base + stage;
+    return base;
+}
+
+}  // namespace sq103
+
+using namespace sq103;
+
+extern "C" {
+
+SQ103_API int sq103_randomize_spins(int8_t *q, int N, int m, uint64_t seed, uint32_t step, int tagSide,
+                                    void *stream) {
+    if (N <= 0 || m <= 0) return kErrBadShape;
+    long long n = (long long)m * ((N + 127) / 128);
+    int blocks = (int)((n + 255) / 256);
+    randomize_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(q, N, m, seed, step,
+                                                               (uint32_t)kTagRandomize | ((uint32_t)tagSide << 8));
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
+    if (!task || task->N <= 0 || task->m <= 0 || task->nSteps < 0) return kErrBadShape;
+    if (task->nSteps == 0) return 0;
+    size_t smem = cta_smem_bytes(task->N, task->m);
+    if (smem > (size_t)max_dyn_smem()) return kErrBadShape;  // flip lists alone do not fit
+    dense_sweep_cta<<<1, kBlockThreads, smem, (cudaStream_t)stream>>>(nullptr, *task, (int)smem);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_anneal_batch(const sq103_dense_task *d_tasks, int nTasks, int maxN, int maxM,
+                                       void *stream) {
+    if (nTasks <= 0) return 0;
+    size_t smem = cta_smem_bytes(maxN, maxM);
+    if (smem > (size_t)max_dyn_smem()) return kErrBadShape;
+    sq103_dense_task dummy = {};
+    dense_sweep_cta<<<nTasks, kBlockThreads, smem, (cudaStream_t)stream>>>(d_tasks, dummy, (int)smem);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

@@ -1,0 +1,315 @@
+// formulas.cu -- QUBO -> Ising conversion, local-field refresh and FP64 energies.
+//
+// Dense QUBO -> Ising (sqaodc/cuda/DeviceFormulas.cpp:24-31 /
+// sqaodc/cpu/SharedFormulas.cpp:36-55):
+//   h_i = -1/2 sum_j W_ij,  J = -W/4 with zero diagonal,
+//   c = sum(-W/4) + sum(diag(-W/4)); maximisation negates W first.
+// Bipartite (sqaodc/cpu/SharedFormulas.cpp:148-167):
+//   J = -W/4 (N1 x N0), h0 = -1/4 colsum(W) - b0/2, h1 = -1/4 rowsum(W) - b1/2,
+//   c = -1/4 sum(W) - 1/2 (sum b0 + sum b1).
+// Sums are accumulated in FP64 with fixed reduction trees (deterministic).
+//
+// spin_gemm: C[y][n] = sum_k q[y][k] * B(k, n) with q in {-1, +1} (int8).
+// Used for the dense field refresh F = q J (J symmetric), the bipartite
+// half-step fields and the energies.  Each output is the FP64 sum, in k order,
+// of fp32 partial sums over 32-wide k chunks (the products are exact), so the
+// result is deterministic and within a few fp32 ulps of the exact sum.
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+// ------------------------------------------------------------ reductions
+template <int BLOCK>
+__device__ double block_sum_f64(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double r = 0.;
+    if (warp == 0) {
+        r = lane < BLOCK / 32 ? red[lane] : 0.;
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    __syncthreads();
+    return r;  // valid in thread 0
+}
+
+// ----------------------------------------------------- dense hamiltonian
+// one block per row: h, J row, per-row contribution to c
+__global__ void __launch_bounds__(256) dg_hamiltonian_rows(const float *W, int ldW, int N, float sign,
+                                                           float *h, float *J, int ldJ, double *rowc) {
+    __shared__ double red[8];
+    int i = blockIdx.x;
+    const float *Wi = W + (size_t)i * ldW;
+    float *Ji = J + (size_t)i * ldJ;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N; j += 256) {
+        float w = sign * Wi[j];
+        s += (double)w;
+        Ji[j] = (j == i) ? 0.f : -0.25f * w;
+    }
+    double rs = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        float wii = sign * Wi[i];
+        h[i] = (float)(-0.5 * rs);
+        rowc[i] = -0.25 * rs + -0.25 * (double)wii;
+    }
+}
+
+// single block: c = sum(rowc) (+ extra), written as fp32 and FP64
+__global__ void __launch_bounds__(256) reduce_constant(const double *parts, int n, double extra, float *c,
+                                                       double *c64) {
+    __shared__ double red[8];
+    double s = 0.;
+    for (int i = threadIdx.x; i < n; i += 256) s += parts[i];
+    double r = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        r += extra;
+        if (c) *c = (float)r;
+        if (c64) *c64 = r;
+    }
+}
+
+// ------------------------------------------------- bipartite hamiltonian
+// one block per row i of W (N1 x N0): J row, h1[i], row part of c
+__global__ void __launch_bounds__(256) bg_hamiltonian_rows(const float *W, int N0, int N1, float sign,
+                                                           const float *b1, float *h1, float *J,
+                                                           double *rowc) {
+    __shared__ double red[8];
+    int i = blockIdx.x;
+    const float *Wi = W + (size_t)i * N0;
+    float *Ji = J + (size_t)i * N0;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N0; j += 256) {
+        float w = sign * Wi[j];
+        s += (double)w;
+        Ji[j] = -0.25f * w;
+    }
+    double rs = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        double bi = (double)(sign * b1[i]);
+        h1[i] = (float)(-0.25 * rs - 0.5 * bi);
+        rowc[i] = -0.25 * rs - 0.5 * bi;
+    }
+}
+
+// one thread per column j: h0[j], column part of c (b0 only)
+__global__ void bg_hamiltonian_cols(const float *W, int N0, int N1, float sign, const float *b0, float *h0,
+                                    double *colc) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N0) return;
+    double s = 0.;
+    for (int i = 0; i < N1; ++i) s += (double)(sign * W[(size_t)i * N0 + j]);
+    double bj = (double)(sign * b0[j]);
+    h0[j] = (float)(-0.25 * s - 0.5 * bj);
+    colc[j] = -0.5 * bj;
+}
+
+// ------------------------------------------------------------ spin GEMM
+// C[y][n] = sum_k A[y][k] B(k, n);  A int8 spins (M x K, lda);
+// TRANS_B = false: B(k, n) = Bm[k * ldb + n];  true: B(k, n) = Bm[n * ldb + k].
+// Block tile 64 x 64, k chunk 32, 256 threads, 4 x 4 outputs per thread.
+template <bool TRANS_B, typename OutT>
+__global__ void __launch_bounds__(256) spin_gemm_kernel(const int8_t *A, int lda, const float *Bm, int ldb,
+                                                        OutT *C, int ldc, int M, int Nn, int K) {
+    __shared__ float As[32][64 + 4];
+    __shared__ float Bs[32][64 + 4];
+    int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    int y0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    double acc[4][4];
+    float part[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.;
+    for (int k0 = 0; k0 < K; k0 += 32) {
+        // A tile: 64 rows (y) x 32 k -> As[k][y]
+        for (int idx = threadIdx.x; idx < 64 * 32; idx += 256) {
+            int r = idx >> 5, kk = idx & 31;
+            int y = y0 + r, k = k0 + kk;
+            As[kk][r] = (y < M && k < K) ? (float)A[(size_t)y * lda + k] : 0.f;
+        }
+        if (!TRANS_B) {
+            for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
+                int kk = idx >> 6, c = idx & 63;
+                int k = k0 + kk, n = n0 + c;
+                Bs[kk][c] = (k < K && n < Nn) ? Bm[(size_t)k * ldb + n] : 0.f;
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < 32 * 64; idx += 256) {
+                int c = idx >> 5, kk = idx & 31;
+                int k = k0 + kk, n = n0 + c;
+                Bs[kk][c] = (k < K && n < Nn) ? Bm[(size_t)n * ldb + k] : 0.f;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) part[a][b] = 0.f;
+#pragma unroll 8
+        for (int kk = 0; kk < 32; ++kk) {
+            float av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = As[kk][ty * 4 + a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx * 4 + b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) part[a][b] = __fmaf_rn(av[a], bv[b], part[a][b]);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        int y = y0 + ty * 4 + a;
+        if (y >= M) continue;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            int n = n0 + tx * 4 + b;
+            if (n < Nn) C[(size_t)y * ldc + n] = (OutT)acc[a][b];
+        }
+    }
+}
+
+template <bool TRANS_B, typename OutT>
+static void launch_spin_gemm(const int8_t *A, int lda, const float *B, int ldb, OutT *C, int ldc, int M,
+                             int Nn, int K, cudaStream_t s) {
+    dim3 grid((Nn + 63) / 64, (M + 63) / 64);
+    spin_gemm_kernel<TRANS_B, OutT><<<grid, 256, 0, s>>>(A, lda, B, ldb, C, ldc, M, Nn, K);
+}
+
+// ------------------------------------------------------------ energies
+// dense: E[y] = -c - sum_i q_yi (h_i + r_yi),  r = q J  (FP64)
+__global__ void __launch_bounds__(256) dg_energy_finish(const int8_t *q, int N, const float *h,
+                                                        const double *r, const double *c64, double sign,
+                                                        double *E64, float *E32) {
+    __shared__ double red[8];
+    int y = blockIdx.x;
+    double s = 0.;
+    for (int i = threadIdx.x; i < N; i += 256) {
+        double qi = q[(size_t)y * N + i];
+        s += qi * ((double)h[i] + r[(size_t)y * N + i]);
+    }
+    double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        double e = sign * (-*c64 - t);
+        if (E64) E64[y] = e;
+        if (E32) E32[y] = (float)e;
+    }
+}
+
+// bipartite: E[y] = -(h0.q0 + h1.q1 + q1.r1) - c, r1 = q0 J^T (FP64)
+__global__ void __launch_bounds__(256) bg_energy_finish(const int8_t *q0, const int8_t *q1, int N0, int N1,
+                                                        const float *h0, const float *h1, const double *r1,
+                                                        const double *c64, double sign, double *E64,
+                                                        float *E32) {
+    __shared__ double red[8];
+    int y = blockIdx.x;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N0; j += 256) s += (double)q0[(size_t)y * N0 + j] * (double)h0[j];
+    for (int i = threadIdx.x; i < N1; i += 256) {
+        double qi = q1[(size_t)y * N1 + i];
+        s += qi * ((double)h1[i] + r1[(size_t)y * N1 + i]);
+    }
+    double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        double e = sign * (-t - *c64);
+        if (E64) E64[y] = e;
+        if (E32) E32[y] = (float)e;
+    }
+}
+
+// spin-ring sum for getSystemE: sum_y sum_i q_yi q_{(y+1)%m, i}
+__global__ void __launch_bounds__(256) ring_dot(const int8_t *q, int N, int m, long long *out) {
+    __shared__ double red[8];
+    long long s = 0;
+    for (size_t idx = (size_t)blockIdx.x * 256 + threadIdx.x; idx < (size_t)m * N;
+         idx += (size_t)gridDim.x * 256) {
+        size_t y = idx / N, i = idx - y * N;
+        size_t y1 = (y + 1) % m;
+        s += (int)q[y * N + i] * (int)q[y1 * N + i];
+    }
+    double t = block_sum_f64<256>((double)s, red);
+    if (threadIdx.x == 0) atomicAdd((unsigned long long *)out, (unsigned long long)(long long)t);
+}
+
+}  // namespace sq103
+
+using namespace sq103;
+
+extern "C" {
+
+SQ103_API int sq103_dense_hamiltonian(const float *W, int ldW, int N, int maximize, float *h, float *J, int ldJ,
+                            float *c, double *c64, double *scratch, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (N <= 0) return kErrBadShape;
+    float sign = maximize ? -1.f : 1.f;
+    dg_hamiltonian_rows<<<N, 256, 0, s>>>(W, ldW, N, sign, h, J, ldJ, scratch);
+    reduce_constant<<<1, 256, 0, s>>>(scratch, N, 0., c, c64);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_hamiltonian(const float *b0, const float *b1, const float *W, int N0, int N1,
+                                int maximize, float *h0, float *h1, float *J, float *c, double *c64,
+                                double *scratch, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (N0 <= 0 || N1 <= 0) return kErrBadShape;
+    float sign = maximize ? -1.f : 1.f;
+    bg_hamiltonian_rows<<<N1, 256, 0, s>>>(W, N0, N1, sign, b1, h1, J, scratch);
+    bg_hamiltonian_cols<<<(N0 + 127) / 128, 128, 0, s>>>(W, N0, N1, sign, b0, h0, scratch + N1);
+    reduce_constant<<<1, 256, 0, s>>>(scratch, N0 + N1, 0., c, c64);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q, float *F, int N, int m,
+                              void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_spin_gemm<false, float>(q, N, J, ldJ, F, N, m, N, N, s);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_fields(const float *J, int N0, int N1, const int8_t *qFixed, int side, float *F, int m,
+                           void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (side == 1)  // F1[y][i] = sum_j J[i][j] q0[y][j]
+        launch_spin_gemm<true, float>(qFixed, N0, J, N0, F, N1, m, N1, N0, s);
+    else  // F0[y][j] = sum_i q1[y][i] J[i][j]
+        launch_spin_gemm<false, float>(qFixed, N1, J, N0, F, N0, m, N0, N1, s);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_energy(const float *J, int ldJ, const float *h, const double *c64, const int8_t *q, int N,
+                       int m, int maximize, double *r_scratch, double *E64, float *E32, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_spin_gemm<false, double>(q, N, J, ldJ, r_scratch, N, m, N, N, s);
+    dg_energy_finish<<<m, 256, 0, s>>>(q, N, h, r_scratch, c64, maximize ? -1. : 1., E64, E32);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const float *h1, const double *c64,
+                           const int8_t *q0, const int8_t *q1, int N0, int N1, int m, int maximize,
+                           double *r_scratch, double *E64, float *E32, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_spin_gemm<true, double>(q0, N0, J, N0, r_scratch, N1, m, N1, N0, s);
+    bg_energy_finish<<<m, 256, 0, s>>>(q0, q1, N0, N1, h0, h1, r_scratch, c64, maximize ? -1. : 1., E64,
+                                       E32);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_ring_dot(const int8_t *q, int N, int m, long long *out, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaMemsetAsync(out, 0, sizeof(long long), s);
+    int blocks = (int)(((size_t)m * N + 255) / 256);
+    if (blocks > 1024) blocks = 1024;
+    ring_dot<<<blocks, 256, 0, s>>>(q, N, m, out);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

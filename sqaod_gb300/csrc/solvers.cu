@@ -1,0 +1,1172 @@
+// solvers.cu -- the sqaod::cuda solver classes (float) on the sm_103a kernels.
+//
+// Behaviour follows the reference's CUDA solvers (state machine, algorithm
+// selection, preference handling, error messages):
+//   dense annealer     sqaodc/cuda/CUDADenseGraphAnnealer.cu:26-375
+//   bipartite annealer sqaodc/cuda/CUDABipartiteGraphAnnealer.cu
+//   dense BF           sqaodc/cuda/CUDADenseGraphBFSearcher.cpp:15-185
+//   bipartite BF       sqaodc/cuda/CUDABipartiteGraphBFSearcher.cpp
+// with these differences, each deliberate:
+//   - the dense annealer also offers algorithm "naive" (the CPU solver's
+//     menu: naive / coloring / sa_naive), as the target API lists it;
+//   - random numbers come from the in-kernel Philox stream
+//     (seed, step counter), so a seeded run replays bit-exactly;
+//   - returned energies are evaluated in FP64 on the GPU;
+//   - BF ties are broken by an FP64 re-evaluation of the candidates; the
+//     result is the first tileSize minimisers in ascending order (the
+//     CUDA reference's append-while-short rule).
+#include <float.h>
+#include <math.h>
+#include <string.h>
+#include <time.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include <sqaodc/sqaodc.h>
+
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+namespace sq = sqaod;
+
+[[noreturn]] static void throw_cuda(int code, const char *what) {
+    sq::throwError("%s failed: %s (%d)", what, code > 0 && code < 1000 ? cudaGetErrorString((cudaError_t)code) : "device status",
+                   code);
+}
+
+static void check(int code, const char *what) {
+    if (code != 0) throw_cuda(code, what);
+}
+#define SQ_CHECK(call) check((int)(call), #call)
+
+// owning device buffer
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void ensure(size_t count) {
+        if (count <= n && p) return;
+        release();
+        if (count == 0) return;
+        SQ_CHECK(cudaMalloc((void **)&p, sizeof(T) * count));
+        n = count;
+    }
+};
+
+// owning pinned host buffer
+template <class T>
+struct HostBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf &) = delete;
+    HostBuf &operator=(const HostBuf &) = delete;
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void ensure(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (count == 0) return;
+        SQ_CHECK(cudaMallocHost((void **)&p, sizeof(T) * count));
+        n = count;
+    }
+};
+
+// solver stream, created on first use so that a solver object can be built
+// (and its preferences and state rules used) before any CUDA work
+struct Stream {
+    cudaStream_t h = nullptr;
+    Stream() = default;
+    Stream(const Stream &) = delete;
+    ~Stream() {
+        if (h) cudaStreamDestroy(h);
+    }
+    cudaStream_t get() {
+        if (!h) SQ_CHECK(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
+        return h;
+    }
+    void sync() { SQ_CHECK(cudaStreamSynchronize(get())); }
+};
+
+class DeviceImpl : public sq::cuda::Device {
+public:
+    explicit DeviceImpl(int devNo) { initialize(devNo < 0 ? 0 : devNo); }
+    void initialize(int devNo) override {
+        devNo_ = devNo;
+        SQ_CHECK(cudaSetDevice(devNo));
+    }
+    void finalize() override {}
+    int devNo_ = 0;
+};
+
+static unsigned long long time_seed() { return (unsigned long long)time(nullptr); }
+
+// ======================================================= dense annealer
+class DenseAnnealer : public sq::cuda::DenseGraphAnnealer<float> {
+public:
+    typedef sq::MatrixType<float> Matrix;
+    typedef sq::VectorType<float> Vector;
+
+    DenseAnnealer() {
+        m_ = -1;
+        selectAlgorithm(sq::algoDefault);
+    }
+
+    void assignDevice(sq::cuda::Device &device) override {
+        SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
+    }
+
+    sq::Algorithm selectAlgorithm(sq::Algorithm algo) override {
+        switch (algo) {
+        case sq::algoNaive:
+        case sq::algoColoring:
+        case sq::algoSANaive:
+            algo_ = algo;
+            break;
+        default:
+            selectDefaultAlgorithm(algo, sq::algoColoring, sq::algoSANaive);
+            break;
+        }
+        return algo_;
+    }
+
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::Annealer<float>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+
+    void seed(unsigned long long s) override {
+        seed_ = s;
+        step_ = 0;
+        setState(solRandSeedGiven);
+    }
+
+    void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
+        throwErrorIf(!sq::isSymmetric(W), "%s, Matrix is not symmetric.", __func__);
+        clearState(solProblemSet);
+        N_ = W.rows;
+        m_ = N_ / 4;
+        om_ = om;
+        allocProblem();
+        DevBuf<float> dW;
+        dW.ensure((size_t)N_ * N_);
+        upload(dW.p, W);
+        SQ_CHECK(sq103_dense_hamiltonian(dW.p, N_, N_, om == sq::optMaximize, d_h_.p, d_J_.p, N_, d_c_.p, d_c64_.p,
+                                         d_scratchN_.p, st_.get()));
+        st_.sync();
+        setState(solProblemSet);
+    }
+
+    void setHamiltonian(const Vector &h, const Matrix &J, float c) override {
+        throwErrorIf(J.rows != J.cols, "%s, J is not a sqare matrix.", __func__);
+        throwErrorIf(h.size != J.cols, "%s, Shape does not match.", __func__);
+        throwErrorIf(!sq::isSymmetric(J), "%s, Matrix is not symmetric.", __func__);
+        clearState(solProblemSet);
+        N_ = J.rows;
+        m_ = N_ / 4;
+        om_ = sq::optMinimize;
+        allocProblem();
+        SQ_CHECK(cudaMemcpyAsync(d_h_.p, h.data, sizeof(float) * N_, cudaMemcpyHostToDevice, st_.get()));
+        upload(d_J_.p, J);
+        double c64 = (double)c;
+        SQ_CHECK(cudaMemcpyAsync(d_c_.p, &c, sizeof(float), cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c64, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();
+        setState(solProblemSet);
+    }
+
+    void getHamiltonian(Vector *h, Matrix *J, float *c) const override {
+        throwErrorIfProblemNotSet();
+        h->resize(N_);
+        J->resize(N_, N_);
+        SQ_CHECK(cudaMemcpyAsync(h->data, d_h_.p, sizeof(float) * N_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpy2DAsync(J->data, sizeof(float) * J->stride, d_J_.p, sizeof(float) * N_, sizeof(float) * N_,
+                                   N_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(c, d_c_.p, sizeof(float), cudaMemcpyDeviceToHost, st_.get()));
+        const_cast<Stream &>(st_).sync();
+    }
+
+    void prepare() override {
+        throwErrorIfProblemNotSet();
+        throwErrorIf(m_ <= 0, "# trotters must be a positive integer.");
+        if (!isRandSeedGiven()) seed(time_seed());
+        setState(solRandSeedGiven);
+        clearState(solPrepared);
+        if (m_ == 1) selectDefaultSAAlgorithm(algo_, sq::algoSANaive);
+        size_t mn = (size_t)m_ * N_;
+        d_q_.ensure(mn);
+        d_F_.ensure(mn);
+        d_E64_.ensure(m_);
+        d_E32_.ensure(m_);
+        h_E64_.ensure(m_);
+        h_q_.ensure(mn);
+        E_.resize(m_);
+        setState(solPrepared);
+    }
+
+    void randomizeSpin() override {
+        throwErrorIfNotPrepared();
+        SQ_CHECK(sq103_randomize_spins(d_q_.p, N_, m_, seed_, step_++, 0, st_.get()));
+        refreshFields();
+        setState(solQSet);
+    }
+
+    void set_q(const sq::BitSet &q) override {
+        throwErrorIfNotPrepared();
+        throwErrorIf(q.size != N_, "Dimension of q, %d, should be equal to N, %d.", q.size, N_);
+        for (int y = 0; y < m_; ++y) memcpy(h_q_.p + (size_t)y * N_, q.data, N_);
+        uploadQ();
+    }
+
+    void set_qset(const sq::BitSetArray &qs) override {
+        throwErrorIfProblemNotSet();
+        for (int i = 0; i < qs.size(); ++i)
+            throwErrorIf(qs[i].size != N_, "%s, Shape does not match.", __func__);
+        throwErrorIf(qs.size() <= 0, "%s, empty q set.", __func__);
+        m_ = qs.size();
+        prepare();
+        for (int y = 0; y < m_; ++y) memcpy(h_q_.p + (size_t)y * N_, qs[y].data, N_);
+        uploadQ();
+    }
+
+    const sq::BitSetArray &get_q() const override {
+        if (!isSolutionAvailable()) const_cast<DenseAnnealer *>(this)->makeSolution();
+        return qlist_;
+    }
+
+    const sq::BitSetArray &get_x() const override {
+        if (!isSolutionAvailable()) const_cast<DenseAnnealer *>(this)->makeSolution();
+        return xlist_;
+    }
+
+    const Vector &get_E() const override {
+        if (!isEAvailable()) const_cast<DenseAnnealer *>(this)->calculate_E();
+        return E_;
+    }
+
+    void calculate_E() override {
+        throwErrorIfQNotSet();
+        d_r_.ensure((size_t)m_ * N_);
+        SQ_CHECK(sq103_dense_energy(d_J_.p, N_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize, d_r_.p,
+                                    d_E64_.p, d_E32_.p, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(h_E64_.p, d_E64_.p, sizeof(double) * m_, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        E_.resize(m_);
+        for (int y = 0; y < m_; ++y) E_(y) = (float)h_E64_.p[y];
+        setState(solEAvailable);
+    }
+
+    void makeSolution() override {
+        throwErrorIfQNotSet();
+        syncBits();
+        setState(solSolutionAvailable);
+        calculate_E();
+    }
+
+    float getSystemE(float G, float beta) const override {
+        auto self = const_cast<DenseAnnealer *>(this);
+        self->calculate_E();
+        double E = 0.;
+        for (int y = 0; y < m_; ++y) E += E_(y);
+        E /= m_;
+        if (sq::isSQAAlgorithm(algo_)) {
+            self->d_ring_.ensure(1);
+            SQ_CHECK(sq103_ring_dot(d_q_.p, N_, m_, self->d_ring_.p, st_.get()));
+            long long ring = 0;
+            SQ_CHECK(cudaMemcpyAsync(&ring, d_ring_.p, sizeof(long long), cudaMemcpyDeviceToHost, st_.get()));
+            self->st_.sync();
+            float coef = 0.5f / beta * std::log(std::tanh(G * beta / (float)m_));
+            E -= (double)ring * coef;
+        }
+        if (om_ == sq::optMaximize) E = -E;
+        return (float)E;
+    }
+
+    void annealOneStep(float G, float beta) override {
+        throwErrorIfNotPrepared();
+        throwErrorIfQNotSet();
+        runSteps(nullptr, nullptr, G, beta, 1);
+    }
+
+    // extension: a whole schedule (host arrays) in one call
+    void anneal(const float *G, const float *beta, int nSteps) {
+        throwErrorIfNotPrepared();
+        throwErrorIfQNotSet();
+        if (nSteps <= 0) return;
+        d_sched_.ensure(2 * (size_t)nSteps);
+        SQ_CHECK(cudaMemcpyAsync(d_sched_.p, G, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_sched_.p + nSteps, beta, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        runSteps(d_sched_.p, d_sched_.p + nSteps, 0.f, 0.f, nSteps);
+    }
+
+    void getE64(std::vector<double> &out) {
+        get_E();
+        out.assign(h_E64_.p, h_E64_.p + m_);
+    }
+    unsigned long long accepted() {
+        if (!d_acc_.p) return 0;
+        unsigned long long v = 0;
+        SQ_CHECK(cudaMemcpyAsync(&v, d_acc_.p, sizeof(v), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        return v;
+    }
+    void rngState(unsigned long long *s, uint32_t *step) const {
+        *s = seed_;
+        *step = step_;
+    }
+    void setTrace(bool on) { trace_ = on; }
+    void getTrace(uint32_t *bits, int nwords) {
+        throwErrorIf(!trace_ || !d_trace_.p, "trace is not enabled.");
+        size_t n = std::min((size_t)nwords, d_trace_.n);
+        SQ_CHECK(cudaMemcpyAsync(bits, d_trace_.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+    }
+    int numTrotters() const { return m_; }
+    int problemSize() const { return N_; }
+
+private:
+    void allocProblem() {
+        d_J_.ensure((size_t)N_ * N_);
+        d_h_.ensure(N_);
+        d_c_.ensure(1);
+        d_c64_.ensure(1);
+        d_scratchN_.ensure(N_);
+    }
+
+    void upload(float *dst, const Matrix &M) {
+        SQ_CHECK(cudaMemcpy2DAsync(dst, sizeof(float) * M.cols, M.data, sizeof(float) * M.stride,
+                                   sizeof(float) * M.cols, M.rows, cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();  // M may be a temporary of the caller
+    }
+
+    void uploadQ() {
+        SQ_CHECK(cudaMemcpyAsync(d_q_.p, h_q_.p, (size_t)m_ * N_, cudaMemcpyHostToDevice, st_.get()));
+        refreshFields();
+        st_.sync();
+        setState(solQSet);
+    }
+
+    void refreshFields() {
+        SQ_CHECK(sq103_dense_field_refresh(d_J_.p, N_, d_q_.p, d_F_.p, N_, m_, st_.get()));
+        stepsSinceRefresh_ = 0;
+    }
+
+    void runSteps(const float *dG, const float *dBeta, float G, float beta, int nSteps) {
+        int algo = algo_ == sq::algoNaive ? kNaive : (algo_ == sq::algoSANaive ? kSANaive : kColoring);
+        d_acc_.ensure(1);
+        if (!accInit_) {
+            SQ_CHECK(cudaMemsetAsync(d_acc_.p, 0, sizeof(unsigned long long), st_.get()));
+            accInit_ = true;
+        }
+        size_t words = ((size_t)N_ * m_ + 31) / 32;
+        if (trace_) {
+            d_trace_.ensure(words * nSteps);
+            SQ_CHECK(cudaMemsetAsync(d_trace_.p, 0, sizeof(uint32_t) * words * nSteps, st_.get()));
+        }
+        // periodic refresh of the resident fields bounds fp32 drift of the rank-1 updates
+        int done = 0;
+        while (done < nSteps) {
+            int chunk = nSteps - done;
+            if (refreshPeriod_ > 0) chunk = std::min(chunk, refreshPeriod_ - stepsSinceRefresh_);
+            if (chunk <= 0) {
+                refreshFields();
+                continue;
+            }
+            sq103_dense_task t = {};
+            t.J = d_J_.p;
+            t.h = d_h_.p;
+            t.q = d_q_.p;
+            t.F = d_F_.p;
+            t.trace = trace_ ? d_trace_.p + words * done : nullptr;
+            t.accepted = d_acc_.p;
+            t.G = dG ? dG + done : nullptr;
+            t.beta = dBeta ? dBeta + done : nullptr;
+            t.Gs = G;
+            t.betas = beta;
+            t.seed = seed_;
+            t.step0 = step_;
+            t.N = N_;
+            t.m = m_;
+            t.ldJ = N_;
+            t.algo = algo;
+            t.nSteps = chunk;
+            SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
+            step_ += (uint32_t)chunk;
+            stepsSinceRefresh_ += chunk;
+            done += chunk;
+        }
+        clearState(solSolutionAvailable);
+    }
+
+    void syncBits() {
+        size_t mn = (size_t)m_ * N_;
+        h_q_.ensure(mn);
+        SQ_CHECK(cudaMemcpyAsync(h_q_.p, d_q_.p, mn, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        qlist_.clear();
+        xlist_.clear();
+        for (int y = 0; y < m_; ++y) {
+            sq::BitSet q(N_);
+            memcpy(q.data, h_q_.p + (size_t)y * N_, N_);
+            xlist_.pushBack(sq::x_from_q(q));
+            qlist_.pushBack(q);
+        }
+    }
+
+    mutable Stream st_;
+    DevBuf<float> d_J_, d_h_, d_c_, d_F_, d_E32_, d_sched_;
+    DevBuf<double> d_c64_, d_scratchN_, d_E64_, d_r_;
+    DevBuf<int8_t> d_q_;
+    DevBuf<unsigned long long> d_acc_;
+    DevBuf<long long> d_ring_;
+    DevBuf<uint32_t> d_trace_;
+    HostBuf<double> h_E64_;
+    HostBuf<int8_t> h_q_;
+    Vector E_;
+    sq::BitSetArray xlist_, qlist_;
+    unsigned long long seed_ = 0;
+    uint32_t step_ = 0;
+    bool trace_ = false, accInit_ = false;
+    int refreshPeriod_ = 8, stepsSinceRefresh_ = 0;
+};
+
+// =================================================== bipartite annealer
+class BipartiteAnnealer : public sq::cuda::BipartiteGraphAnnealer<float> {
+public:
+    typedef sq::MatrixType<float> Matrix;
+    typedef sq::VectorType<float> Vector;
+
+    BipartiteAnnealer() {
+        m_ = -1;
+        selectAlgorithm(sq::algoDefault);
+    }
+
+    void assignDevice(sq::cuda::Device &device) override {
+        SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
+    }
+
+    sq::Algorithm selectAlgorithm(sq::Algorithm algo) override {
+        switch (algo) {
+        case sq::algoNaive:
+        case sq::algoColoring:
+        case sq::algoSANaive:
+        case sq::algoSAColoring:
+            algo_ = algo;
+            break;
+        default:
+            selectDefaultAlgorithm(algo, sq::algoColoring, sq::algoSAColoring);
+            break;
+        }
+        return algo_;
+    }
+
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::Annealer<float>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+
+    void seed(unsigned long long s) override {
+        seed_ = s;
+        step_ = 0;
+        setState(solRandSeedGiven);
+    }
+
+    void setQUBO(const Vector &b0, const Vector &b1, const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.cols != b0.size || W.rows != b1.size, "%s, Shape does not match.", __func__);
+        clearState(solProblemSet);
+        N0_ = b0.size;
+        N1_ = b1.size;
+        m_ = (N0_ + N1_) / 4;
+        om_ = om;
+        allocProblem();
+        DevBuf<float> db0, db1, dW;
+        db0.ensure(N0_);
+        db1.ensure(N1_);
+        dW.ensure((size_t)N0_ * N1_);
+        SQ_CHECK(cudaMemcpyAsync(db0.p, b0.data, sizeof(float) * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(db1.p, b1.data, sizeof(float) * N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpy2DAsync(dW.p, sizeof(float) * N0_, W.data, sizeof(float) * W.stride, sizeof(float) * N0_, N1_,
+                                   cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(sq103_bipartite_hamiltonian(db0.p, db1.p, dW.p, N0_, N1_, om == sq::optMaximize, d_h0_.p, d_h1_.p,
+                                             d_J_.p, d_c_.p, d_c64_.p, d_scratch_.p, st_.get()));
+        st_.sync();
+        setState(solProblemSet);
+    }
+
+    void setHamiltonian(const Vector &h0, const Vector &h1, const Matrix &J, float c) override {
+        throwErrorIf(J.cols != h0.size || J.rows != h1.size, "%s, Shape does not match.", __func__);
+        clearState(solProblemSet);
+        N0_ = h0.size;
+        N1_ = h1.size;
+        m_ = (N0_ + N1_) / 4;
+        om_ = sq::optMinimize;
+        allocProblem();
+        double c64 = c;
+        SQ_CHECK(cudaMemcpyAsync(d_h0_.p, h0.data, sizeof(float) * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_h1_.p, h1.data, sizeof(float) * N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpy2DAsync(d_J_.p, sizeof(float) * N0_, J.data, sizeof(float) * J.stride, sizeof(float) * N0_,
+                                   N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_c_.p, &c, sizeof(float), cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c64, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();
+        setState(solProblemSet);
+    }
+
+    void getHamiltonian(Vector *h0, Vector *h1, Matrix *J, float *c) const override {
+        throwErrorIfProblemNotSet();
+        h0->resize(N0_);
+        h1->resize(N1_);
+        J->resize(N1_, N0_);
+        SQ_CHECK(cudaMemcpyAsync(h0->data, d_h0_.p, sizeof(float) * N0_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(h1->data, d_h1_.p, sizeof(float) * N1_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpy2DAsync(J->data, sizeof(float) * J->stride, d_J_.p, sizeof(float) * N0_, sizeof(float) * N0_,
+                                   N1_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(c, d_c_.p, sizeof(float), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+    }
+
+    void prepare() override {
+        throwErrorIfProblemNotSet();
+        throwErrorIf(m_ <= 0, "# trotters must be a positive integer.");
+        if (!isRandSeedGiven()) seed(time_seed());
+        setState(solRandSeedGiven);
+        clearState(solPrepared);
+        if (m_ == 1) selectDefaultSAAlgorithm(algo_, sq::algoSAColoring);
+        d_q0_.ensure((size_t)m_ * N0_);
+        d_q1_.ensure((size_t)m_ * N1_);
+        d_F0_.ensure((size_t)m_ * N0_);
+        d_F1_.ensure((size_t)m_ * N1_);
+        d_E64_.ensure(m_);
+        h_E64_.ensure(m_);
+        h_q0_.ensure((size_t)m_ * N0_);
+        h_q1_.ensure((size_t)m_ * N1_);
+        E_.resize(m_);
+        setState(solPrepared);
+    }
+
+    void randomizeSpin() override {
+        throwErrorIfNotPrepared();
+        uint32_t step = step_++;
+        SQ_CHECK(sq103_randomize_spins(d_q0_.p, N0_, m_, seed_, step, 0, st_.get()));
+        SQ_CHECK(sq103_randomize_spins(d_q1_.p, N1_, m_, seed_, step, 1, st_.get()));
+        setState(solQSet);
+    }
+
+    void set_q(const sq::BitSetPair &qp) override {
+        throwErrorIfNotPrepared();
+        throwErrorIf(qp.bits0.size != N0_, "Dimension of q0, %d,  should be equal to N0, %d.", qp.bits0.size, N0_);
+        throwErrorIf(qp.bits1.size != N1_, "Dimension of q1, %d,  should be equal to N1, %d.", qp.bits1.size, N1_);
+        for (int y = 0; y < m_; ++y) {
+            memcpy(h_q0_.p + (size_t)y * N0_, qp.bits0.data, N0_);
+            memcpy(h_q1_.p + (size_t)y * N1_, qp.bits1.data, N1_);
+        }
+        uploadQ();
+    }
+
+    void set_qset(const sq::BitSetPairArray &qs) override {
+        throwErrorIfProblemNotSet();
+        throwErrorIf(qs.size() <= 0, "%s, empty q set.", __func__);
+        for (int i = 0; i < qs.size(); ++i)
+            throwErrorIf(qs[i].bits0.size != N0_ || qs[i].bits1.size != N1_, "%s, Shape does not match.", __func__);
+        m_ = qs.size();
+        prepare();
+        for (int y = 0; y < m_; ++y) {
+            memcpy(h_q0_.p + (size_t)y * N0_, qs[y].bits0.data, N0_);
+            memcpy(h_q1_.p + (size_t)y * N1_, qs[y].bits1.data, N1_);
+        }
+        uploadQ();
+    }
+
+    const sq::BitSetPairArray &get_q() const override {
+        if (!isSolutionAvailable()) const_cast<BipartiteAnnealer *>(this)->makeSolution();
+        return qlist_;
+    }
+    const sq::BitSetPairArray &get_x() const override {
+        if (!isSolutionAvailable()) const_cast<BipartiteAnnealer *>(this)->makeSolution();
+        return xlist_;
+    }
+    const Vector &get_E() const override {
+        if (!isEAvailable()) const_cast<BipartiteAnnealer *>(this)->calculate_E();
+        return E_;
+    }
+
+    void calculate_E() override {
+        throwErrorIfQNotSet();
+        d_r_.ensure((size_t)m_ * N1_);
+        SQ_CHECK(sq103_bipartite_energy(d_J_.p, d_h0_.p, d_h1_.p, d_c64_.p, d_q0_.p, d_q1_.p, N0_, N1_, m_,
+                                        om_ == sq::optMaximize, d_r_.p, d_E64_.p, nullptr, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(h_E64_.p, d_E64_.p, sizeof(double) * m_, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        E_.resize(m_);
+        for (int y = 0; y < m_; ++y) E_(y) = (float)h_E64_.p[y];
+        setState(solEAvailable);
+    }
+
+    void makeSolution() override {
+        throwErrorIfNotPrepared();
+        throwErrorIfQNotSet();
+        syncBits();
+        setState(solSolutionAvailable);
+        calculate_E();
+    }
+
+    float getSystemE(float G, float beta) const override {
+        auto self = const_cast<BipartiteAnnealer *>(this);
+        self->calculate_E();
+        double E = 0.;
+        for (int y = 0; y < m_; ++y) E += E_(y);
+        E /= m_;
+        if (sq::isSQAAlgorithm(algo_)) {
+            self->d_ring_.ensure(2);
+            SQ_CHECK(sq103_ring_dot(d_q0_.p, N0_, m_, self->d_ring_.p, st_.get()));
+            SQ_CHECK(sq103_ring_dot(d_q1_.p, N1_, m_, self->d_ring_.p + 1, st_.get()));
+            long long ring[2] = {0, 0};
+            SQ_CHECK(cudaMemcpyAsync(ring, d_ring_.p, sizeof(ring), cudaMemcpyDeviceToHost, st_.get()));
+            self->st_.sync();
+            float coef = 0.5f / beta * std::log(std::tanh(G * beta / (float)m_));
+            E -= (double)(ring[0] + ring[1]) * coef;
+        }
+        if (om_ == sq::optMaximize) E = -E;
+        return (float)E;
+    }
+
+    void annealOneStep(float G, float beta) override {
+        throwErrorIfNotPrepared();
+        throwErrorIfQNotSet();
+        runSteps(nullptr, nullptr, G, beta, 1);
+    }
+
+    void anneal(const float *G, const float *beta, int nSteps) {
+        throwErrorIfNotPrepared();
+        throwErrorIfQNotSet();
+        if (nSteps <= 0) return;
+        d_sched_.ensure(2 * (size_t)nSteps);
+        SQ_CHECK(cudaMemcpyAsync(d_sched_.p, G, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_sched_.p + nSteps, beta, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        runSteps(d_sched_.p, d_sched_.p + nSteps, 0.f, 0.f, nSteps);
+    }
+
+    void getE64(std::vector<double> &out) {
+        get_E();
+        out.assign(h_E64_.p, h_E64_.p + m_);
+    }
+    unsigned long long accepted() {
+        if (!d_acc_.p) return 0;
+        unsigned long long v = 0;
+        SQ_CHECK(cudaMemcpyAsync(&v, d_acc_.p, sizeof(v), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        return v;
+    }
+    void rngState(unsigned long long *s, uint32_t *step) const {
+        *s = seed_;
+        *step = step_;
+    }
+    void setTrace(bool on) { trace_ = on; }
+    void getTrace(uint32_t *bits, int nwords) {
+        throwErrorIf(!trace_ || !d_trace_.p, "trace is not enabled.");
+        size_t n = std::min((size_t)nwords, d_trace_.n);
+        SQ_CHECK(cudaMemcpyAsync(bits, d_trace_.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+    }
+    int numTrotters() const { return m_; }
+
+private:
+    void allocProblem() {
+        d_J_.ensure((size_t)N0_ * N1_);
+        d_h0_.ensure(N0_);
+        d_h1_.ensure(N1_);
+        d_c_.ensure(1);
+        d_c64_.ensure(1);
+        d_scratch_.ensure(N0_ + N1_);
+    }
+
+    void uploadQ() {
+        SQ_CHECK(cudaMemcpyAsync(d_q0_.p, h_q0_.p, (size_t)m_ * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_q1_.p, h_q1_.p, (size_t)m_ * N1_, cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();
+        setState(solQSet);
+    }
+
+    void runSteps(const float *dG, const float *dBeta, float G, float beta, int nSteps) {
+        int algo = algo_ == sq::algoNaive ? kNaive
+                   : algo_ == sq::algoSANaive ? kSANaive
+                   : algo_ == sq::algoSAColoring ? kSAColoring
+                                                  : kColoring;
+        d_acc_.ensure(1);
+        if (!accInit_) {
+            SQ_CHECK(cudaMemsetAsync(d_acc_.p, 0, sizeof(unsigned long long), st_.get()));
+            accInit_ = true;
+        }
+        size_t perStep = (size_t)m_ * (N0_ + N1_);
+        if (algo == kNaive) perStep = (size_t)(N0_ + N1_) * m_;
+        if (algo == kSANaive) perStep = (size_t)(N0_ + N1_) * m_ * m_;
+        size_t words = (perStep + 31) / 32;
+        if (trace_) {
+            d_trace_.ensure(words * nSteps);
+            SQ_CHECK(cudaMemsetAsync(d_trace_.p, 0, sizeof(uint32_t) * words * nSteps, st_.get()));
+        }
+        sq103_bipartite_task t = {};
+        t.J = d_J_.p;
+        t.h0 = d_h0_.p;
+        t.h1 = d_h1_.p;
+        t.q0 = d_q0_.p;
+        t.q1 = d_q1_.p;
+        t.F0 = d_F0_.p;
+        t.F1 = d_F1_.p;
+        t.trace = trace_ ? d_trace_.p : nullptr;
+        t.accepted = d_acc_.p;
+        t.G = dG;
+        t.beta = dBeta;
+        t.Gs = G;
+        t.betas = beta;
+        t.seed = seed_;
+        t.step0 = step_;
+        t.N0 = N0_;
+        t.N1 = N1_;
+        t.m = m_;
+        t.algo = algo;
+        t.nSteps = nSteps;
+        SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
+        step_ += (uint32_t)nSteps;
+        clearState(solSolutionAvailable);
+    }
+
+    void syncBits() {
+        SQ_CHECK(cudaMemcpyAsync(h_q0_.p, d_q0_.p, (size_t)m_ * N0_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(h_q1_.p, d_q1_.p, (size_t)m_ * N1_, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        qlist_.clear();
+        xlist_.clear();
+        for (int y = 0; y < m_; ++y) {
+            sq::BitSet q0(N0_), q1(N1_);
+            memcpy(q0.data, h_q0_.p + (size_t)y * N0_, N0_);
+            memcpy(q1.data, h_q1_.p + (size_t)y * N1_, N1_);
+            xlist_.pushBack(sq::BitSetPair(sq::x_from_q(q0), sq::x_from_q(q1)));
+            qlist_.pushBack(sq::BitSetPair(q0, q1));
+        }
+    }
+
+    mutable Stream st_;
+    DevBuf<float> d_J_, d_h0_, d_h1_, d_c_, d_F0_, d_F1_, d_sched_;
+    DevBuf<double> d_c64_, d_scratch_, d_E64_, d_r_;
+    DevBuf<int8_t> d_q0_, d_q1_;
+    DevBuf<unsigned long long> d_acc_;
+    DevBuf<long long> d_ring_;
+    DevBuf<uint32_t> d_trace_;
+    HostBuf<double> h_E64_;
+    HostBuf<int8_t> h_q0_, h_q1_;
+    Vector E_;
+    sq::BitSetPairArray xlist_, qlist_;
+    unsigned long long seed_ = 0;
+    uint32_t step_ = 0;
+    bool trace_ = false, accInit_ = false;
+};
+
+// ========================================================== BF searchers
+// Running result of a brute-force search: exact FP64 minimum and the first
+// `cap` minimisers in ascending order of the packed value.
+template <class Key>
+struct BfResult {
+    double Emin = DBL_MAX;
+    std::vector<Key> xs;
+    void reset() {
+        Emin = DBL_MAX;
+        xs.clear();
+    }
+    // merge candidates (with FP64 energies) of a range that comes after every range merged so far
+    void merge(const std::vector<Key> &cand, const std::vector<double> &E, size_t cap) {
+        double m = DBL_MAX;
+        for (double e : E) m = std::min(m, e);
+        if (cand.empty()) return;
+        std::vector<Key> sel;
+        for (size_t i = 0; i < cand.size(); ++i)
+            if (E[i] == m) sel.push_back(cand[i]);
+        std::sort(sel.begin(), sel.end());
+        if (m < Emin) {
+            Emin = m;
+            xs.clear();
+        } else if (m > Emin) {
+            return;
+        }
+        for (size_t i = 0; i < sel.size() && xs.size() < cap; ++i) xs.push_back(sel[i]);
+    }
+};
+
+struct Pair {
+    uint64_t x0, x1;
+    bool operator<(const Pair &o) const { return x0 != o.x0 ? x0 < o.x0 : x1 < o.x1; }
+};
+
+static float bf_slack(const std::vector<float> &vals) {
+    bool integer = true;
+    double s = 0.;
+    for (float v : vals) {
+        if (v != std::floor(v)) integer = false;
+        s += std::fabs((double)v);
+    }
+    if (integer && s < 16777216.) return 0.f;
+    return (float)(16. * s * 5.96e-8);
+}
+
+class DenseBFSearcher : public sq::cuda::DenseGraphBFSearcher<float> {
+public:
+    typedef sq::MatrixType<float> Matrix;
+    typedef sq::VectorType<float> Vector;
+
+    DenseBFSearcher() { tileSize_ = 1 << 18; }
+
+    void assignDevice(sq::cuda::Device &device) override {
+        SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
+    }
+
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::DenseGraphBFSearcher<float>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+
+    void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
+        throwErrorIf(!sq::isSymmetric(W), "%s, Matrix is not symmetric.", __func__);
+        throwErrorIf(63 < W.rows, "N must be smaller than 64, N=%d.", W.rows);
+        clearState(solProblemSet);
+        N_ = W.rows;
+        om_ = om;
+        W_.assign((size_t)N_ * N_, 0.f);
+        float sgn = om == sq::optMaximize ? -1.f : 1.f;
+        for (int r = 0; r < N_; ++r)
+            for (int c = 0; c < N_; ++c) W_[(size_t)r * N_ + c] = sgn * W(r, c);
+        setState(solProblemSet);
+    }
+
+    void prepare() override {
+        throwErrorIfProblemNotSet();
+        x_ = 0;
+        xMax_ = 1ull << N_;
+        if (xMax_ < (sq::PackedBitSet)tileSize_) tileSize_ = (sq::SizeType)xMax_;
+        d_W_.ensure((size_t)N_ * N_);
+        SQ_CHECK(cudaMemcpyAsync(d_W_.p, W_.data(), sizeof(float) * N_ * N_, cudaMemcpyHostToDevice, st_.get()));
+        d_ws_.ensure(sq103_bf_workspace_bytes(N_));
+        slack_ = bf_slack(W_);
+        res_.reset();
+        xList_.clear();
+        st_.sync();
+        setState(solPrepared);
+    }
+
+    bool searchRange(sq::PackedBitSet *curXEnd) override {
+        throwErrorIfNotPrepared();
+        clearState(solSolutionAvailable);
+        uint64_t b = x_, e = std::min<uint64_t>(x_ + tileSize_, xMax_);
+        if (b < e) runRange(b, e);
+        x_ = e;
+        if (curXEnd) *curXEnd = x_;
+        return x_ == xMax_;
+    }
+
+    // whole-range fast path: same result as prepare() + searchRange() until done + makeSolution()
+    void search() override {
+        prepare();
+        const uint64_t chunk = 1ull << 34;
+        for (uint64_t b = 0; b < xMax_; b += chunk) runRange(b, std::min<uint64_t>(xMax_, b + chunk));
+        x_ = xMax_;
+        makeSolution();
+    }
+
+    void calculate_E() override {
+        throwErrorIfNotPrepared();
+        E_.resize(xList_.size() ? xList_.size() : 1);
+        float E = (float)res_.Emin;
+        if (res_.Emin == DBL_MAX) E = FLT_MAX;
+        E_ = (om_ == sq::optMaximize) ? -E : E;
+        setState(solEAvailable);
+    }
+
+    void makeSolution() override {
+        throwErrorIfNotPrepared();
+        xList_.clear();
+        size_t n = std::min(res_.xs.size(), (size_t)tileSize_);
+        for (size_t i = 0; i < n; ++i) {
+            sq::BitSet bits;
+            sq::unpackBitSet(&bits, res_.xs[i], N_);
+            xList_.pushBack(bits);
+        }
+        setState(solSolutionAvailable);
+        calculate_E();
+    }
+
+    const sq::BitSetArray &get_x() const override {
+        if (!isSolutionAvailable()) const_cast<DenseBFSearcher *>(this)->makeSolution();
+        return xList_;
+    }
+    const Vector &get_E() const override {
+        if (!isEAvailable()) const_cast<DenseBFSearcher *>(this)->calculate_E();
+        return E_;
+    }
+    double EminExact() const { return om_ == sq::optMaximize ? -res_.Emin : res_.Emin; }
+
+private:
+    // one range in ascending order; splits itself when the candidates overflow
+    void runRange(uint64_t b, uint64_t e) {
+        int cap = (int)std::min<uint64_t>(std::max<uint64_t>((uint64_t)tileSize_, 1u << 16), 1u << 22);
+        d_cand_.ensure(cap);
+        int count = 0;
+        float emin32 = 0.f;
+        SQ_CHECK(sq103_dense_bf_range(d_W_.p, N_, b, e, slack_, d_ws_.p, d_cand_.p, cap, &count, &emin32, st_.get()));
+        if (count > cap) {
+            uint64_t mid = b + (e - b) / 2;
+            runRange(b, mid);
+            // with exact energies every candidate of a heavy tie equals Emin: stop once the list is full
+            if (slack_ == 0.f && res_.xs.size() >= (size_t)tileSize_ && (double)emin32 >= res_.Emin) return;
+            runRange(mid, e);
+            return;
+        }
+        std::vector<uint64_t> cand(count);
+        std::vector<double> E(count);
+        if (count > 0) {
+            d_E_.ensure(count);
+            SQ_CHECK(sq103_dense_bf_refine(d_W_.p, N_, d_cand_.p, count, d_E_.p, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(cand.data(), d_cand_.p, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(E.data(), d_E_.p, sizeof(double) * count, cudaMemcpyDeviceToHost, st_.get()));
+            st_.sync();
+        }
+        res_.merge(cand, E, (size_t)tileSize_);
+    }
+
+    Stream st_;
+    std::vector<float> W_;
+    DevBuf<float> d_W_;
+    DevBuf<unsigned char> d_ws_;
+    DevBuf<uint64_t> d_cand_;
+    DevBuf<double> d_E_;
+    BfResult<uint64_t> res_;
+    float slack_ = 0.f;
+    sq::BitSetArray xList_;
+    Vector E_;
+};
+
+class BipartiteBFSearcher : public sq::cuda::BipartiteGraphBFSearcher<float> {
+public:
+    typedef sq::MatrixType<float> Matrix;
+    typedef sq::VectorType<float> Vector;
+
+    BipartiteBFSearcher() {
+        tileSize0_ = 8192;
+        tileSize1_ = 8192;
+    }
+
+    void assignDevice(sq::cuda::Device &device) override {
+        SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
+    }
+
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::BipartiteGraphBFSearcher<float>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+
+    void setQUBO(const Vector &b0, const Vector &b1, const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.cols != b0.size || W.rows != b1.size, "%s, Shape does not match.", __func__);
+        throwErrorIf(63 < b0.size, "N0 must be smaller than 64, N0=%d.", b0.size);
+        throwErrorIf(63 < b1.size, "N1 must be smaller than 64, N1=%d.", b1.size);
+        clearState(solProblemSet);
+        N0_ = b0.size;
+        N1_ = b1.size;
+        om_ = om;
+        float sgn = om == sq::optMaximize ? -1.f : 1.f;
+        b0_.resize(N0_);
+        b1_.resize(N1_);
+        W_.resize((size_t)N0_ * N1_);
+        for (int j = 0; j < N0_; ++j) b0_[j] = sgn * b0(j);
+        for (int i = 0; i < N1_; ++i) b1_[i] = sgn * b1(i);
+        for (int i = 0; i < N1_; ++i)
+            for (int j = 0; j < N0_; ++j) W_[(size_t)i * N0_ + j] = sgn * W(i, j);
+        setState(solProblemSet);
+    }
+
+    void prepare() override {
+        throwErrorIfProblemNotSet();
+        x0_ = x1_ = 0;
+        x0max_ = 1ull << N0_;
+        x1max_ = 1ull << N1_;
+        if (x0max_ < (sq::PackedBitSet)tileSize0_) tileSize0_ = (sq::SizeType)x0max_;
+        if (x1max_ < (sq::PackedBitSet)tileSize1_) tileSize1_ = (sq::SizeType)x1max_;
+        d_b0_.ensure(N0_);
+        d_b1_.ensure(N1_);
+        d_W_.ensure((size_t)N0_ * N1_);
+        SQ_CHECK(cudaMemcpyAsync(d_b0_.p, b0_.data(), sizeof(float) * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_b1_.p, b1_.data(), sizeof(float) * N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_W_.p, W_.data(), sizeof(float) * N0_ * N1_, cudaMemcpyHostToDevice, st_.get()));
+        d_ws_.ensure(sq103_bf_workspace_bytes(N0_ + N1_));
+        std::vector<float> all(W_);
+        all.insert(all.end(), b0_.begin(), b0_.end());
+        all.insert(all.end(), b1_.begin(), b1_.end());
+        slack_ = bf_slack(all);
+        res_.reset();
+        xList_.clear();
+        st_.sync();
+        setState(solPrepared);
+    }
+
+    // tiles advance x1 first, then x0 (CUDABipartiteGraphBFSearcher.cpp:168-211)
+    bool searchRange(sq::PackedBitSet *curX0, sq::PackedBitSet *curX1) override {
+        throwErrorIfNotPrepared();
+        clearState(solSolutionAvailable);
+        uint64_t b0 = x0_, e0 = std::min<uint64_t>(x0_ + tileSize0_, x0max_);
+        uint64_t b1 = x1_, e1 = std::min<uint64_t>(x1_ + tileSize1_, x1max_);
+        if (b0 < e0 && b1 < e1) runRange(b0, e0, b1, e1);
+        x1_ = e1;
+        if (x1_ == x1max_) {
+            x1_ = 0;
+            x0_ = std::min<uint64_t>(x0_ + tileSize0_, x0max_);
+        }
+        if (curX0) *curX0 = x0_;
+        if (curX1) *curX1 = x1_;
+        return x0_ == x0max_;
+    }
+
+    void search() override {
+        prepare();
+        runRange(0, x0max_, 0, x1max_);
+        x0_ = x0max_;
+        x1_ = 0;
+        makeSolution();
+    }
+
+    void calculate_E() override {
+        throwErrorIfNotPrepared();
+        E_.resize(xList_.size() ? xList_.size() : 1);
+        float E = res_.Emin == DBL_MAX ? FLT_MAX : (float)res_.Emin;
+        E_ = (om_ == sq::optMaximize) ? -E : E;
+        setState(solEAvailable);
+    }
+
+    void makeSolution() override {
+        throwErrorIfNotPrepared();
+        xList_.clear();
+        // result order: ascending (x0, x1); at most tileSize0 + tileSize1 pairs
+        // (the merge cap of CPUBipartiteGraphBFSearcher.cpp:117-151)
+        std::vector<Pair> xs = res_.xs;
+        std::sort(xs.begin(), xs.end());
+        size_t n = std::min(xs.size(), (size_t)(tileSize0_ + tileSize1_));
+        for (size_t i = 0; i < n; ++i) {
+            sq::BitSet a, b;
+            sq::unpackBitSet(&a, xs[i].x0, N0_);
+            sq::unpackBitSet(&b, xs[i].x1, N1_);
+            xList_.pushBack(sq::BitSetPair(a, b));
+        }
+        setState(solSolutionAvailable);
+        calculate_E();
+    }
+
+    const sq::BitSetPairArray &get_x() const override {
+        if (!isSolutionAvailable()) const_cast<BipartiteBFSearcher *>(this)->makeSolution();
+        return xList_;
+    }
+    const Vector &get_E() const override {
+        if (!isEAvailable()) const_cast<BipartiteBFSearcher *>(this)->calculate_E();
+        return E_;
+    }
+
+private:
+    void runRange(uint64_t b0, uint64_t e0, uint64_t b1, uint64_t e1) {
+        int cap = 1 << 20;
+        d_cand_.ensure(2 * (size_t)cap);
+        int count = 0;
+        float emin32 = 0.f;
+        SQ_CHECK(sq103_bipartite_bf_range(d_b0_.p, d_b1_.p, d_W_.p, N0_, N1_, b0, e0, b1, e1, slack_, d_ws_.p,
+                                          d_cand_.p, cap, &count, &emin32, st_.get()));
+        if (count > cap) {
+            // split the x1 range (or x0 when x1 is a single value)
+            if (e1 - b1 > 1) {
+                uint64_t mid = b1 + (e1 - b1) / 2;
+                runRange(b0, e0, b1, mid);
+                runRange(b0, e0, mid, e1);
+            } else {
+                uint64_t mid = b0 + (e0 - b0) / 2;
+                runRange(b0, mid, b1, e1);
+                runRange(mid, e0, b1, e1);
+            }
+            return;
+        }
+        std::vector<uint64_t> raw(2 * (size_t)count);
+        std::vector<double> E(count);
+        if (count > 0) {
+            d_E_.ensure(count);
+            SQ_CHECK(sq103_bipartite_bf_refine(d_b0_.p, d_b1_.p, d_W_.p, N0_, N1_, d_cand_.p, count, d_E_.p, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(raw.data(), d_cand_.p, sizeof(uint64_t) * 2 * count, cudaMemcpyDeviceToHost, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(E.data(), d_E_.p, sizeof(double) * count, cudaMemcpyDeviceToHost, st_.get()));
+            st_.sync();
+        }
+        std::vector<Pair> cand(count);
+        for (int i = 0; i < count; ++i) cand[i] = Pair{raw[2 * i], raw[2 * i + 1]};
+        // ranges of one search are not visited in (x0, x1) order: keep all ties, cap at the end
+        res_.merge(cand, E, (size_t)1 << 24);
+    }
+
+    Stream st_;
+    std::vector<float> b0_, b1_, W_;
+    DevBuf<float> d_b0_, d_b1_, d_W_;
+    DevBuf<unsigned char> d_ws_;
+    DevBuf<uint64_t> d_cand_;
+    DevBuf<double> d_E_;
+    BfResult<Pair> res_;
+    float slack_ = 0.f;
+    sq::BitSetPairArray xList_;
+    Vector E_;
+};
+
+}  // namespace sq103
+
+// ============================================================ factories
+namespace sqaod {
+namespace cuda {
+
+template <>
+DenseGraphAnnealer<float> *newDenseGraphAnnealer<float>() {
+    return new sq103::DenseAnnealer();
+}
+template <>
+BipartiteGraphAnnealer<float> *newBipartiteGraphAnnealer<float>() {
+    return new sq103::BipartiteAnnealer();
+}
+template <>
+DenseGraphBFSearcher<float> *newDenseGraphBFSearcher<float>() {
+    return new sq103::DenseBFSearcher();
+}
+template <>
+BipartiteGraphBFSearcher<float> *newBipartiteGraphBFSearcher<float>() {
+    return new sq103::BipartiteBFSearcher();
+}
+Device *newDevice(int devNo) { return new sq103::DeviceImpl(devNo); }
+
+}  // namespace cuda
+}  // namespace sqaod
+
+extern "C" SQ103_API void sqaodc_cuda_version(int *version, int *cuda_version) {
+    *version = 10003;
+    int v = 0;
+    cudaRuntimeGetVersion(&v);
+    *cuda_version = v;
+}
+
+#include "capi_impl.inc"

@@ -1,0 +1,491 @@
+"""CUDA solvers of the sqaod Python API on libsqaod_gb300.so.
+
+Same classes, factory functions, method names and argument meanings as
+sqaodpy/sqaod/cuda/{dense_graph_annealer,bipartite_graph_annealer,
+dense_graph_bf_searcher,bipartite_graph_bf_searcher}.py over the base
+classes of sqaodpy/sqaod/common/*_base.py.  Every method forwards to one
+handle-layer entry point of the C ABI (include/sqaod_gb300.h).
+
+Only dtype=numpy.float32 is provided; other dtypes raise.
+"""
+import ctypes
+
+import numpy as np
+
+from .. import common
+from .._lib import call, lib, ptr
+
+_c_int = ctypes.c_int
+_c_float = ctypes.c_float
+
+
+def _check_dtype(dtype):
+    if dtype is None:
+        return np.float32
+    if np.dtype(dtype) != np.float32:
+        raise RuntimeError("dtype %s is not provided: this build computes in float32 only." % np.dtype(dtype))
+    return np.float32
+
+
+def _pref_value(v):
+    if isinstance(v, bool):
+        return str(int(v))
+    return str(v)
+
+
+def _parse_prefs(s):
+    out = {}
+    for item in s.split(';'):
+        if not item:
+            continue
+        k, v = item.split('=', 1)
+        if k in ('n_trotters', 'tile_size', 'tile_size_0', 'tile_size_1'):
+            v = int(v)
+        out[k] = v
+    return out
+
+
+class _Handle:
+    _prefix = None
+
+    def __init__(self):
+        self._L = lib()
+        h = ctypes.c_void_p()
+        call(self._fn('new'), ctypes.byref(h))
+        self._h = h
+
+    def _fn(self, name):
+        return getattr(self._L, '%s_%s' % (self._prefix, name))
+
+    def _call(self, name, *args):
+        return call(self._fn(name), self._h, *args)
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and h.value:
+            try:
+                self._fn('delete')(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def set_preferences(self, prefdict=None, **prefs):
+        merged = {}
+        if prefdict is not None:
+            merged.update(prefdict)
+        merged.update(prefs)
+        for k, v in merged.items():
+            self._call('set_preference', str(k).encode(), _pref_value(v).encode())
+
+    def get_preferences(self):
+        buf = ctypes.create_string_buffer(512)
+        self._call('get_preferences', buf, _c_int(512))
+        return _parse_prefs(buf.value.decode())
+
+    def get_optimize_dir(self):
+        return self._optimize
+
+
+class DenseGraphAnnealer(_Handle):
+    """Dense-graph annealer (sqaodpy/sqaod/common/dense_graph_annealer_base.py)."""
+    _prefix = 'sq103_dg_annealer'
+
+    def __init__(self, W, optimize, dtype, prefdict):
+        self.dtype = _check_dtype(dtype)
+        super().__init__()
+        self._optimize = common.minimize
+        if W is not None:
+            self.set_qubo(W, optimize)
+        self.set_preferences(prefdict)
+
+    def seed(self, seed):
+        self._call('seed', ctypes.c_ulonglong(int(seed)))
+
+    def set_qubo(self, W, optimize=common.minimize):
+        common.check_square(W)
+        W = common.fix_type(W, self.dtype)
+        W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
+        self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        self._optimize = optimize
+
+    def set_hamiltonian(self, h, J, c):
+        common.check_square(J, 'J')
+        h, J = common.fix_type([np.asarray(h), np.asarray(J)], self.dtype)
+        J = np.ascontiguousarray(common.symmetrize(J), self.dtype)
+        self._call('set_hamiltonian', ptr(h), ptr(J), _c_float(float(c)), _c_int(J.shape[0]))
+        self._optimize = common.minimize
+
+    def get_problem_size(self):
+        n = _c_int()
+        self._call('get_problem_size', ctypes.byref(n))
+        return n.value
+
+    def _m(self):
+        return self.get_preferences()['n_trotters']
+
+    def get_E(self):
+        cap = max(self._m(), 1)
+        E = np.zeros(cap, np.float32)
+        n = _c_int()
+        self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def get_E64(self):
+        """FP64 energies of the trotters (extension)."""
+        cap = max(self._m(), 1)
+        E = np.zeros(cap, np.float64)
+        n = _c_int()
+        self._call('get_E64', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def calculate_E(self):
+        self._call('calculate_E')
+
+    def _bits(self, name):
+        N, m = self.get_problem_size(), max(self._m(), 1)
+        out = np.zeros((m, N), np.int8)
+        n = _c_int()
+        self._call(name, ptr(out), _c_int(m), ctypes.byref(n))
+        return [out[i].copy() for i in range(n.value)]
+
+    def get_x(self):
+        return self._bits('get_x')
+
+    def get_q(self):
+        return self._bits('get_q')
+
+    def set_q(self, q):
+        q = common.fix_type(np.asarray(q), np.int8)
+        self._call('set_q', ptr(q), _c_int(q.shape[-1]))
+
+    def set_qset(self, qset):
+        qs = np.ascontiguousarray(np.array([common.fix_type(np.asarray(v), np.int8) for v in qset]), np.int8)
+        self._call('set_qset', ptr(qs), _c_int(qs.shape[0]), _c_int(qs.shape[1]))
+
+    def get_hamiltonian(self):
+        N = self.get_problem_size()
+        h = np.empty(N, self.dtype)
+        J = np.empty((N, N), self.dtype)
+        c = np.empty(1, self.dtype)
+        self._call('get_hamiltonian', ptr(h), ptr(J), ptr(c))
+        return h, J, c[0]
+
+    def randomize_spin(self):
+        self._call('randomize_spin')
+
+    def prepare(self):
+        self._call('prepare')
+
+    def init_anneal(self):
+        """prepare() + randomize_spin()."""
+        self._call('init_anneal')
+
+    def make_solution(self):
+        self._call('make_solution')
+
+    def get_system_E(self, G, beta):
+        E = _c_float()
+        self._call('get_system_E', _c_float(G), _c_float(beta), ctypes.byref(E))
+        return np.float32(E.value)
+
+    def anneal_one_step(self, G, beta):
+        self._call('anneal_one_step', _c_float(G), _c_float(beta))
+
+    def anneal(self, G, beta):
+        """Runs len(G) annealOneStep steps in one call (extension)."""
+        G = np.ascontiguousarray(G, np.float32)
+        beta = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float32), G.shape), np.float32)
+        self._call('anneal', ptr(G), ptr(beta), _c_int(len(G)))
+
+    def get_accepted(self):
+        v = ctypes.c_ulonglong()
+        self._call('get_accepted', ctypes.byref(v))
+        return v.value
+
+    def get_rng_state(self):
+        s, st = ctypes.c_ulonglong(), ctypes.c_uint32()
+        self._call('get_rng_state', ctypes.byref(s), ctypes.byref(st))
+        return s.value, st.value
+
+    def set_trace(self, enable):
+        self._call('set_trace', _c_int(1 if enable else 0))
+
+    def get_trace(self, nwords):
+        out = np.zeros(nwords, np.uint32)
+        self._call('get_trace', ptr(out), _c_int(nwords))
+        return out
+
+
+class BipartiteGraphAnnealer(_Handle):
+    """Bipartite-graph annealer (sqaodpy/sqaod/common/bipartite_graph_annealer_base.py)."""
+    _prefix = 'sq103_bg_annealer'
+
+    def __init__(self, b0, b1, W, optimize, dtype, prefdict):
+        self.dtype = _check_dtype(dtype)
+        super().__init__()
+        self._optimize = common.minimize
+        if W is not None:
+            self.set_qubo(b0, b1, W, optimize)
+        self.set_preferences(prefdict)
+
+    def seed(self, seed):
+        self._call('seed', ctypes.c_ulonglong(int(seed)))
+
+    def set_qubo(self, b0, b1, W, optimize=common.minimize):
+        b0, b1, W = common.fix_type([np.asarray(b0), np.asarray(b1), np.asarray(W)], self.dtype)
+        if W.ndim != 2 or W.shape != (len(b1), len(b0)):
+            raise RuntimeError('dimension mismatch for b0, b1, W.')
+        self._call('set_qubo', ptr(b0), ptr(b1), ptr(W), _c_int(len(b0)), _c_int(len(b1)),
+                   _c_int(common.optimize_flag(optimize)))
+        self._optimize = optimize
+
+    def set_hamiltonian(self, h0, h1, J, c):
+        h0, h1, J = common.fix_type([np.asarray(h0), np.asarray(h1), np.asarray(J)], self.dtype)
+        if J.ndim != 2 or J.shape != (len(h1), len(h0)):
+            raise RuntimeError('dimension mismatch for h0, h1, J.')
+        self._call('set_hamiltonian', ptr(h0), ptr(h1), ptr(J), _c_float(float(c)), _c_int(len(h0)),
+                   _c_int(len(h1)))
+        self._optimize = common.minimize
+
+    def get_problem_size(self):
+        a, b = _c_int(), _c_int()
+        self._call('get_problem_size', ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def _m(self):
+        return self.get_preferences()['n_trotters']
+
+    def get_E(self):
+        cap = max(self._m(), 1)
+        E = np.zeros(cap, np.float32)
+        n = _c_int()
+        self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def get_E64(self):
+        cap = max(self._m(), 1)
+        E = np.zeros(cap, np.float64)
+        n = _c_int()
+        self._call('get_E64', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def calculate_E(self):
+        self._call('calculate_E')
+
+    def _pairs(self, name):
+        (N0, N1), m = self.get_problem_size(), max(self._m(), 1)
+        a = np.zeros((m, N0), np.int8)
+        b = np.zeros((m, N1), np.int8)
+        n = _c_int()
+        self._call(name, ptr(a), ptr(b), _c_int(m), ctypes.byref(n))
+        return [(a[i].copy(), b[i].copy()) for i in range(n.value)]
+
+    def get_x(self):
+        return self._pairs('get_x')
+
+    def get_q(self):
+        return self._pairs('get_q')
+
+    def set_q(self, qpair):
+        q0, q1 = (common.fix_type(np.asarray(v), np.int8) for v in qpair)
+        self._call('set_q', ptr(q0), ptr(q1), _c_int(len(q0)), _c_int(len(q1)))
+
+    def set_qset(self, qset):
+        q0 = np.ascontiguousarray(np.array([np.asarray(p[0], np.int8) for p in qset]), np.int8)
+        q1 = np.ascontiguousarray(np.array([np.asarray(p[1], np.int8) for p in qset]), np.int8)
+        self._call('set_qset', ptr(q0), ptr(q1), _c_int(q0.shape[0]), _c_int(q0.shape[1]), _c_int(q1.shape[1]))
+
+    def get_hamiltonian(self):
+        N0, N1 = self.get_problem_size()
+        h0 = np.empty(N0, self.dtype)
+        h1 = np.empty(N1, self.dtype)
+        J = np.empty((N1, N0), self.dtype)
+        c = np.empty(1, self.dtype)
+        self._call('get_hamiltonian', ptr(h0), ptr(h1), ptr(J), ptr(c))
+        return h0, h1, J, c[0]
+
+    def randomize_spin(self):
+        self._call('randomize_spin')
+
+    def prepare(self):
+        self._call('prepare')
+
+    def init_anneal(self):
+        self._call('init_anneal')
+
+    def make_solution(self):
+        self._call('make_solution')
+
+    def get_system_E(self, G, beta):
+        E = _c_float()
+        self._call('get_system_E', _c_float(G), _c_float(beta), ctypes.byref(E))
+        return np.float32(E.value)
+
+    def anneal_one_step(self, G, beta):
+        self._call('anneal_one_step', _c_float(G), _c_float(beta))
+
+    def anneal(self, G, beta):
+        G = np.ascontiguousarray(G, np.float32)
+        beta = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float32), G.shape), np.float32)
+        self._call('anneal', ptr(G), ptr(beta), _c_int(len(G)))
+
+    def get_accepted(self):
+        v = ctypes.c_ulonglong()
+        self._call('get_accepted', ctypes.byref(v))
+        return v.value
+
+    def get_rng_state(self):
+        s, st = ctypes.c_ulonglong(), ctypes.c_uint32()
+        self._call('get_rng_state', ctypes.byref(s), ctypes.byref(st))
+        return s.value, st.value
+
+    def set_trace(self, enable):
+        self._call('set_trace', _c_int(1 if enable else 0))
+
+    def get_trace(self, nwords):
+        out = np.zeros(nwords, np.uint32)
+        self._call('get_trace', ptr(out), _c_int(nwords))
+        return out
+
+
+class DenseGraphBFSearcher(_Handle):
+    """Dense-graph brute-force searcher (sqaodpy/sqaod/common/dense_graph_bf_searcher_base.py)."""
+    _prefix = 'sq103_dg_bf'
+
+    def __init__(self, W, optimize, dtype, prefdict):
+        self.dtype = _check_dtype(dtype)
+        super().__init__()
+        self._optimize = common.minimize
+        if W is not None:
+            self.set_qubo(W, optimize)
+        self.set_preferences(prefdict)
+
+    def set_qubo(self, W, optimize=common.minimize):
+        common.check_square(W)
+        W = common.fix_type(W, self.dtype)
+        W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
+        self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        self._optimize = optimize
+
+    def get_problem_size(self):
+        n = _c_int()
+        self._call('get_problem_size', ctypes.byref(n))
+        return n.value
+
+    def _cap(self):
+        return max(self.get_preferences()['tile_size'], 1)
+
+    def get_E(self):
+        cap = self._cap()
+        E = np.zeros(cap, np.float32)
+        n = _c_int()
+        self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def get_x(self):
+        N, cap = self.get_problem_size(), self._cap()
+        out = np.zeros((cap, N), np.int8)
+        n = _c_int()
+        self._call('get_x', ptr(out), _c_int(cap), ctypes.byref(n))
+        return [out[i].copy() for i in range(n.value)]
+
+    def prepare(self):
+        self._call('prepare')
+
+    def calculate_E(self):
+        self._call('calculate_E')
+
+    def make_solution(self):
+        self._call('make_solution')
+
+    def search_range(self):
+        x = ctypes.c_ulonglong()
+        done = _c_int()
+        self._call('search_range', ctypes.byref(x), ctypes.byref(done))
+        return bool(done.value)
+
+    def search(self):
+        self._call('search')
+
+
+class BipartiteGraphBFSearcher(_Handle):
+    """Bipartite-graph brute-force searcher (sqaodpy/sqaod/common/bipartite_graph_bf_searcher_base.py)."""
+    _prefix = 'sq103_bg_bf'
+
+    def __init__(self, b0, b1, W, optimize, dtype, prefdict):
+        self.dtype = _check_dtype(dtype)
+        super().__init__()
+        self._optimize = common.minimize
+        if W is not None:
+            self.set_qubo(b0, b1, W, optimize)
+        self.set_preferences(prefdict)
+
+    def set_qubo(self, b0, b1, W, optimize=common.minimize):
+        b0, b1, W = common.fix_type([np.asarray(b0), np.asarray(b1), np.asarray(W)], self.dtype)
+        if W.ndim != 2 or W.shape != (len(b1), len(b0)):
+            raise RuntimeError('dimension mismatch for b0, b1, W.')
+        self._call('set_qubo', ptr(b0), ptr(b1), ptr(W), _c_int(len(b0)), _c_int(len(b1)),
+                   _c_int(common.optimize_flag(optimize)))
+        self._optimize = optimize
+
+    def get_problem_size(self):
+        a, b = _c_int(), _c_int()
+        self._call('get_problem_size', ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def _cap(self):
+        p = self.get_preferences()
+        return max(p['tile_size_0'] + p['tile_size_1'], 1)
+
+    def get_E(self):
+        cap = self._cap()
+        E = np.zeros(cap, np.float32)
+        n = _c_int()
+        self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        return E[:n.value].copy()
+
+    def get_x(self):
+        (N0, N1), cap = self.get_problem_size(), self._cap()
+        a = np.zeros((cap, N0), np.int8)
+        b = np.zeros((cap, N1), np.int8)
+        n = _c_int()
+        self._call('get_x', ptr(a), ptr(b), _c_int(cap), ctypes.byref(n))
+        return [(a[i].copy(), b[i].copy()) for i in range(n.value)]
+
+    def prepare(self):
+        self._call('prepare')
+
+    def calculate_E(self):
+        self._call('calculate_E')
+
+    def make_solution(self):
+        self._call('make_solution')
+
+    def search_range(self):
+        x0, x1 = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        done = _c_int()
+        self._call('search_range', ctypes.byref(x0), ctypes.byref(x1), ctypes.byref(done))
+        return bool(done.value)
+
+    def search(self):
+        self._call('search')
+
+
+def dense_graph_annealer(W=None, optimize=common.minimize, dtype=np.float32, **prefs):
+    """Factory of DenseGraphAnnealer (sqaodpy/sqaod/cuda/dense_graph_annealer.py:18-31)."""
+    return DenseGraphAnnealer(W, optimize, dtype, prefs)
+
+
+def bipartite_graph_annealer(b0=None, b1=None, W=None, optimize=common.minimize, dtype=np.float32, **prefs):
+    """Factory of BipartiteGraphAnnealer (sqaodpy/sqaod/cuda/bipartite_graph_annealer.py)."""
+    return BipartiteGraphAnnealer(b0, b1, W, optimize, dtype, prefs)
+
+
+def dense_graph_bf_searcher(W=None, optimize=common.minimize, dtype=np.float32, **prefs):
+    """Factory of DenseGraphBFSearcher (sqaodpy/sqaod/cuda/dense_graph_bf_searcher.py)."""
+    return DenseGraphBFSearcher(W, optimize, dtype, prefs)
+
+
+def bipartite_graph_bf_searcher(b0=None, b1=None, W=None, optimize=common.minimize, dtype=np.float32, **prefs):
+    """Factory of BipartiteGraphBFSearcher (sqaodpy/sqaod/cuda/bipartite_graph_bf_searcher.py)."""
+    return BipartiteGraphBFSearcher(b0, b1, W, optimize, dtype, prefs)

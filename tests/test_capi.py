@@ -1,0 +1,133 @@
+"""CPU-only checks of the C ABI library and of the host-side logic.
+
+The library must build, load without a GPU and export every entry point that
+include/sqaod_gb300.h declares; solver objects must apply the reference's
+preference and state rules (sqaodc/common/Solver.cpp, Preference.cpp) before
+any device work.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sqaod_gb300 import _lib
+    return _lib.lib()
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "sqaod_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(sq103_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_symbols()
+    assert len(names) > 60
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_cpp_api_symbols_exported(lib):
+    # the C++ factories of include/sqaodc/sqaodc.h are exported for C++ callers
+    import subprocess
+    from sqaod_gb300 import build
+    out = subprocess.run(["nm", "-DC", "--defined-only", build.lib_path()], capture_output=True, text=True).stdout
+    for sym in ("sqaod::cuda::newDenseGraphAnnealer<float>", "sqaod::cuda::newBipartiteGraphAnnealer<float>",
+                "sqaod::cuda::newDenseGraphBFSearcher<float>", "sqaod::cuda::newBipartiteGraphBFSearcher<float>",
+                "sqaod::deleteInstance", "sqaod::cuda::newDevice"):
+        assert sym in out, sym
+
+
+def test_version(lib):
+    assert lib.sq103_version() == 10003
+
+
+def test_annealer_preferences_on_host():
+    import sqaod_gb300 as sq
+    a = sq.cuda.dense_graph_annealer()
+    p = a.get_preferences()
+    assert p["algorithm"] == "coloring" and p["precision"] == "float" and p["device"] == "cuda"
+    a.set_preferences(algorithm=sq.algorithm.naive, n_trotters=7)
+    p = a.get_preferences()
+    assert p["algorithm"] == "naive" and p["n_trotters"] == 7
+    a.set_preferences(algorithm=sq.algorithm.sa_default)
+    assert a.get_preferences()["algorithm"] == "sa_naive"
+    a.set_preferences(algorithm=sq.algorithm.sa_coloring)
+    assert a.get_preferences()["algorithm"] == "sa_naive"
+    a.set_preferences(algorithm=sq.algorithm.default)
+    assert a.get_preferences()["algorithm"] == "coloring"
+    b = sq.cuda.bipartite_graph_annealer()
+    b.set_preferences(algorithm=sq.algorithm.sa_default)
+    assert b.get_preferences()["algorithm"] == "sa_coloring"
+    b.set_preferences(algorithm=sq.algorithm.naive)
+    assert b.get_preferences()["algorithm"] == "naive"
+
+
+def test_searcher_preferences_on_host():
+    import sqaod_gb300 as sq
+    s = sq.cuda.dense_graph_bf_searcher()
+    p = s.get_preferences()
+    assert p["algorithm"] == "brute_force_search" and p["tile_size"] == 1 << 18
+    s.set_preferences(tile_size=1000)  # rounded up to a multiple of 256
+    assert s.get_preferences()["tile_size"] == 1024
+    s.set_preferences(algorithm=sq.algorithm.naive)
+    assert s.get_preferences()["algorithm"] == "brute_force_search"
+    b = sq.cuda.bipartite_graph_bf_searcher()
+    b.set_preferences(tile_size_0=300, tile_size_1=512)
+    p = b.get_preferences()
+    assert p["tile_size_0"] == 512 and p["tile_size_1"] == 512
+
+
+def test_state_machine_errors_on_host():
+    import sqaod_gb300 as sq
+    a = sq.cuda.dense_graph_annealer()
+    for call in (a.prepare, a.randomize_spin, lambda: a.anneal_one_step(1., 1.), a.calculate_E,
+                 a.make_solution):
+        with pytest.raises(RuntimeError):
+            call()
+    with pytest.raises(RuntimeError):
+        a.set_preferences(n_trotters=0)
+    with pytest.raises(RuntimeError):
+        a.set_preferences(no_such_pref=1)
+    s = sq.cuda.dense_graph_bf_searcher()
+    with pytest.raises(RuntimeError):
+        s.search_range()
+
+
+def test_input_checks_on_host():
+    import sqaod_gb300 as sq
+    with pytest.raises(RuntimeError):
+        sq.cuda.dense_graph_annealer(dtype=np.float64)
+    a = sq.cuda.dense_graph_annealer()
+    W = np.random.default_rng(0).uniform(-1, 1, (6, 6)).astype(np.float32)
+    with pytest.raises(RuntimeError):  # neither symmetric nor triangular
+        a.set_qubo(W)
+    with pytest.raises(RuntimeError):
+        a.set_qubo(np.zeros((3, 4), np.float32))
+    with pytest.raises(RuntimeError):  # N > 63 for a brute-force searcher
+        sq.cuda.dense_graph_bf_searcher().set_qubo(np.zeros((64, 64), np.float32))
+    with pytest.raises(RuntimeError):
+        sq.cuda.bipartite_graph_annealer().set_qubo(np.zeros(3), np.zeros(4), np.zeros((3, 3)))
+
+
+def test_symmetrize_rules():
+    import sqaod_gb300 as sq
+    W = np.triu(np.arange(16, dtype=np.float32).reshape(4, 4))
+    S = sq.symmetrize(W)
+    assert np.allclose(S, S.T) and np.allclose(np.diag(S), np.diag(W))
+    assert sq.symmetrize(S) is S
+
+
+def test_generators_match_reference_draws(golden):
+    """generate_random_symmetric_W draws like sqaodpy's (same np.random calls)."""
+    import sqaod_gb300 as sq
+    np.random.seed(0)
+    W = sq.generate_random_symmetric_W(16)
+    assert np.allclose(np.rint(W * 16384) / 16384., golden["dg_r16_W"])
+    assert np.array_equal(sq.create_bitset_sequence([5], 4), np.array([[0, 1, 0, 1]], np.int8))

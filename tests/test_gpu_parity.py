@@ -1,0 +1,425 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle.
+
+- QUBO -> Ising (h, J, c) and FP64 energies within 1e-5 relative of the FP64
+  oracle and of the reference numpy golden vectors;
+- every annealer sweep replays against the FP64 host replay of the same
+  Philox stream: each decision must agree unless its acceptance margin
+  |min(1, exp(-rate dE)) - u| is below 1e-6 (those are counted);
+- brute-force Emin and argmin sets bit-exact with the reference CPU searcher
+  on integer-valued W;
+- the reference tests' known answers (sqaodpy/tests/test_dense_graph_annealer.py,
+  test_bipartite_graph_annealer.py, test_dense_graph_bf_searcher.py).
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5      # formulas / energies vs FP64
+MARGIN_TOL = 1e-6   # replay: decisions may differ only below this acceptance margin
+
+
+@pytest.fixture(scope="module")
+def sq():
+    import sqaod_gb300
+    return sqaod_gb300
+
+
+def rand_sym(rng, N, lo=-1., hi=1.):
+    W = rng.uniform(lo, hi, (N, N))
+    W = np.triu(W) + np.triu(W, 1).T
+    return W.astype(np.float32)
+
+
+def bits_to_int(bits):
+    v = 0
+    for b in bits:
+        v = (v << 1) | int(b)
+    return v
+
+
+def rel_close(a, b, tol=REL_TOL):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    scale = max(1.0, float(np.max(np.abs(b))) if b.size else 1.0)
+    return float(np.max(np.abs(a - b))) <= tol * scale if b.size else True
+
+
+# ------------------------------------------------------------- formulas
+@pytest.mark.parametrize("om", [0, 1])
+def test_dense_hamiltonian_vs_fp64(sq, orc, om):
+    rng = np.random.default_rng(11)
+    W = rand_sym(rng, 100)
+    a = sq.cuda.dense_graph_annealer(W, sq.maximize if om else sq.minimize)
+    h, J, c = a.get_hamiltonian()
+    h0, J0, c0 = orc.dg_hamiltonian(-W.astype(np.float64) if om else W)
+    assert rel_close(h, h0) and rel_close(J, J0) and rel_close([c], [c0])
+
+
+def test_dense_hamiltonian_golden(sq, golden):
+    for name in ("ex8", "r16", "r100"):
+        a = sq.cuda.dense_graph_annealer(golden["dg_%s_W" % name].astype(np.float32))
+        h, J, c = a.get_hamiltonian()
+        assert rel_close(h, golden["dg_%s_h" % name]) and rel_close(J, golden["dg_%s_J" % name])
+        assert rel_close([c], [golden["dg_%s_c" % name]])
+
+
+def test_dense_energy_all_states_golden(sq, golden):
+    W, X = golden["dg_r8_W"].astype(np.float32), golden["dg_r8_X"]
+    a = sq.cuda.dense_graph_annealer(W)
+    a.set_qset([sq.bit_to_spin(x).astype(np.int8) for x in X])
+    assert rel_close(a.get_E(), golden["dg_r8_E"])
+    assert rel_close(a.get_E64(), golden["dg_r8_E"])
+
+
+def test_dense_energy_vs_fp64_large(sq, orc):
+    rng = np.random.default_rng(5)
+    N, m = 300, 12
+    W = rand_sym(rng, N)
+    a = sq.cuda.dense_graph_annealer(W, n_trotters=m)
+    a.seed(1)
+    a.prepare()
+    a.randomize_spin()
+    q = np.array(a.get_q())
+    h, J, c = orc.dg_hamiltonian(W)
+    assert rel_close(a.get_E64(), orc.dg_energy_ising(h, J, c, q), 1e-9)
+    assert rel_close(a.get_E(), orc.dg_energy_ising(h, J, c, q))
+
+
+def test_known_energies(sq):
+    N = 8
+    a = sq.cuda.dense_graph_annealer(np.ones((N, N), np.float32), n_trotters=1)
+    a.prepare()
+    a.set_q(np.ones(N, np.int8))
+    E = a.get_E()
+    assert len(E) == 1 and E[0] == N * N
+    assert np.all(a.get_x()[0] == 1)
+    a.set_q(-np.ones(N, np.int8))
+    assert abs(a.get_E()[0]) < 1e-6
+    b = sq.cuda.bipartite_graph_annealer(np.ones(4, np.float32), np.ones(4, np.float32),
+                                         np.ones((4, 4), np.float32), n_trotters=1)
+    b.prepare()
+    b.set_q((np.ones(4, np.int8), np.ones(4, np.int8)))
+    assert b.get_E()[0] == 4 * 4 + 4 + 4
+
+
+def test_bipartite_formulas_golden(sq, golden):
+    g = golden
+    b = sq.cuda.bipartite_graph_annealer(g["bg_b0"], g["bg_b1"], g["bg_W"])
+    h0, h1, J, c = b.get_hamiltonian()
+    assert rel_close(h0, g["bg_h0"]) and rel_close(h1, g["bg_h1"]) and rel_close(J, g["bg_J"])
+    assert rel_close([c], [g["bg_c"]])
+    q0 = (2 * g["bg_x0"] - 1).astype(np.int8)
+    q1 = (2 * g["bg_x1"] - 1).astype(np.int8)
+    b.set_qset(list(zip(q0, q1)))
+    assert rel_close(b.get_E(), g["bg_E"])
+
+
+def test_bipartite_hamiltonian_vs_fp64_maximize(sq, orc):
+    rng = np.random.default_rng(3)
+    N0, N1 = 70, 45
+    b0, b1 = rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32)
+    W = rng.uniform(-1, 1, (N1, N0)).astype(np.float32)
+    b = sq.cuda.bipartite_graph_annealer(b0, b1, W, sq.maximize)
+    h0, h1, J, c = b.get_hamiltonian()
+    r = orc.bg_hamiltonian(-b0.astype(np.float64), -b1.astype(np.float64), -W.astype(np.float64))
+    assert rel_close(h0, r[0]) and rel_close(h1, r[1]) and rel_close(J, r[2]) and rel_close([c], [r[3]])
+
+
+# ---------------------------------------------------------- sweep replay
+DENSE_ALGOS = {"coloring": 1, "naive": 0, "sa_naive": 2}
+
+
+@pytest.mark.parametrize("algo", ["coloring", "naive", "sa_naive"])
+@pytest.mark.parametrize("N,m", [(48, 8), (37, 7), (64, 2)])
+def test_dense_sweep_replays_fp64(sq, orc, algo, N, m):
+    rng = np.random.default_rng(N * 100 + m)
+    W = rand_sym(rng, N)
+    a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm=algo)
+    seed = 1234 + N
+    a.seed(seed)
+    a.prepare()
+    a.randomize_spin()
+    q = np.array(a.get_q())
+    assert np.array_equal(q, orc.gpu_randomize(seed, 0, 0, m, N))
+    h, J, c = a.get_hamiltonian()
+    a.set_trace(True)
+    nwords = (N * m + 31) // 32
+    schedule = [(3.0, 10.0), (1.0, 10.0), (0.3, 20.0), (0.05, 50.0)]
+    for G, beta in schedule:
+        _, step = a.get_rng_state()
+        a.anneal_one_step(G, beta)
+        trace = a.get_trace(nwords)
+        q_host, st = orc.dg_replay(h, J, m, DENSE_ALGOS[algo], seed, step, G, beta, q, trace, MARGIN_TOL)
+        q = np.array(a.get_q())
+        assert np.array_equal(q, q_host), "device state diverged from the replayed trace"
+        assert st["n_trials"] == N * m
+        assert st["n_mismatch"] == st["n_mismatch_small"], st
+
+
+BIP_ALGOS = {"naive": 0, "coloring": 1, "sa_naive": 2, "sa_coloring": 3}
+
+
+@pytest.mark.parametrize("algo", ["coloring", "sa_coloring", "naive", "sa_naive"])
+@pytest.mark.parametrize("N0,N1,m", [(40, 24, 6), (17, 33, 5)])
+def test_bipartite_sweep_replays_fp64(sq, orc, algo, N0, N1, m):
+    rng = np.random.default_rng(N0 * 7 + N1 + m)
+    b0, b1 = rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32)
+    W = rng.uniform(-1, 1, (N1, N0)).astype(np.float32)
+    a = sq.cuda.bipartite_graph_annealer(b0, b1, W, n_trotters=m, algorithm=algo)
+    seed = 99 + m
+    a.seed(seed)
+    a.prepare()
+    a.randomize_spin()
+    pairs = a.get_q()
+    q0 = np.array([p[0] for p in pairs])
+    q1 = np.array([p[1] for p in pairs])
+    assert np.array_equal(q0, orc.gpu_randomize(seed, 0, 0, m, N0))
+    assert np.array_equal(q1, orc.gpu_randomize(seed, 0, 1, m, N1))
+    h0, h1, J, c = a.get_hamiltonian()
+    a.set_trace(True)
+    nbits = m * (N0 + N1) * (m if algo == "sa_naive" else 1)
+    for G, beta in [(3.0, 10.0), (0.5, 20.0), (0.05, 50.0)]:
+        _, step = a.get_rng_state()
+        a.anneal_one_step(G, beta)
+        trace = a.get_trace((nbits + 31) // 32)
+        r0, r1, st = orc.bg_replay(h0, h1, J, m, BIP_ALGOS[algo], seed, step, G, beta, q0, q1, trace,
+                                   MARGIN_TOL)
+        pairs = a.get_q()
+        q0 = np.array([p[0] for p in pairs])
+        q1 = np.array([p[1] for p in pairs])
+        assert np.array_equal(q0, r0) and np.array_equal(q1, r1)
+        assert st["n_mismatch"] == st["n_mismatch_small"], st
+
+
+def test_dense_anneal_schedule_equals_steps(sq):
+    """anneal(G[], beta[]) in one call == the same annealOneStep calls (bit-exact)."""
+    rng = np.random.default_rng(8)
+    W = rand_sym(rng, 96)
+    G = [5.0 * 0.9 ** k for k in range(20)]
+    res = []
+    for batched in (False, True):
+        a = sq.cuda.dense_graph_annealer(W, n_trotters=12)
+        a.seed(5)
+        a.prepare()
+        a.randomize_spin()
+        if batched:
+            a.anneal(np.array(G, np.float32), 20.0)
+        else:
+            for g in G:
+                a.anneal_one_step(g, 20.0)
+        res.append((np.array(a.get_q()), a.get_E64()))
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+
+
+# ------------------------------------------------------ known-answer anneals
+def _anneal(a, sq):
+    a.prepare()
+    a.randomize_spin()
+    algo = a.get_preferences()["algorithm"]
+    if algo in ("sa_naive", "sa_coloring"):
+        Ginit, Gfin, beta = 10., 0.02, 1.
+    else:
+        Ginit, Gfin, beta = 5., 0.02, 1. / 0.03
+    nSteps = 100
+    tau = math.exp(math.log(Gfin / Ginit) / nSteps)
+    G = Ginit
+    for _ in range(nSteps):
+        a.anneal_one_step(G, beta)
+        G *= tau
+
+
+@pytest.mark.parametrize("algo,m", [("naive", 4), ("coloring", 4), ("default", 4), ("sa_naive", 1),
+                                    ("default", 1)])
+def test_dense_anneal_known_answers(sq, algo, m):
+    N = 10
+    a = sq.cuda.dense_graph_annealer(np.ones((N, N), np.float32), sq.minimize, n_trotters=m, algorithm=algo)
+    a.seed(42)
+    _anneal(a, sq)
+    assert a.get_E().min() == 0
+    a = sq.cuda.dense_graph_annealer(-np.ones((N, N), np.float32), sq.maximize, n_trotters=m, algorithm=algo)
+    a.seed(43)
+    _anneal(a, sq)
+    assert a.get_E().max() == 0
+    h, J, c = (v.astype(np.float32) if hasattr(v, "astype") else v for v in
+               _py_hamiltonian(np.ones((N, N))))
+    a = sq.cuda.dense_graph_annealer(n_trotters=m)
+    a.set_hamiltonian(h, J, c)
+    a.set_preferences(n_trotters=m, algorithm=algo)
+    a.seed(44)
+    _anneal(a, sq)
+    assert a.get_E().max() == 0
+
+
+def _py_hamiltonian(W):
+    from oracle import oracle_ctypes
+    return oracle_ctypes.dg_hamiltonian(W)
+
+
+@pytest.mark.parametrize("algo", ["naive", "coloring", "default", "sa_coloring", "sa_naive"])
+def test_bipartite_anneal_known_answers(sq, algo):
+    N0, N1, m = 10, 8, 6
+    ones = lambda *s: np.ones(s, np.float32)
+    a = sq.cuda.bipartite_graph_annealer(ones(N0), ones(N1), ones(N1, N0), sq.minimize, n_trotters=m,
+                                         algorithm=algo)
+    a.seed(7)
+    _anneal(a, sq)
+    assert a.get_E().min() == 0
+    a = sq.cuda.bipartite_graph_annealer(-ones(N0), -ones(N1), -ones(N1, N0), sq.maximize, n_trotters=m,
+                                         algorithm=algo)
+    a.seed(8)
+    _anneal(a, sq)
+    assert a.get_E().max() == 0
+
+
+# ----------------------------------------------------------- solver API
+def test_calling_sequence_and_state(sq):
+    rng = np.random.default_rng(1)
+    N, m = 200, 100
+    a = sq.cuda.dense_graph_annealer(rand_sym(rng, N), n_trotters=m, algorithm=sq.algorithm.default)
+    a.seed(0)
+    a.prepare()
+    a.randomize_spin()
+    a.anneal_one_step(1, 1)
+    a.calculate_E()
+    a.get_system_E(1, 1)
+    a.make_solution()
+    assert len(a.get_E()) == m and len(a.get_x()) == m and len(a.get_q()) == m
+    assert a.get_problem_size() == N
+    h, J, c = a.get_hamiltonian()
+    assert h.shape == (N,) and J.shape == (N, N)
+    b = sq.cuda.dense_graph_annealer(rand_sym(rng, 10), n_trotters=10)
+    with pytest.raises(RuntimeError):
+        b.anneal_one_step(0., 0.)
+
+
+def test_set_q_roundtrip(sq):
+    rng = np.random.default_rng(2)
+    N, m = 100, 100
+    a = sq.cuda.dense_graph_annealer(rand_sym(rng, N), n_trotters=m)
+    a.prepare()
+    qin = (2 * rng.integers(0, 2, N) - 1).astype(np.int8)
+    a.set_q(qin)
+    assert all(np.array_equal(qin, q) for q in a.get_q())
+    qs = [(2 * rng.integers(0, 2, 5) - 1).astype(np.int8) for _ in range(2)]
+    b = sq.cuda.dense_graph_annealer(rand_sym(rng, 5), n_trotters=2)
+    b.set_qset(qs)
+    assert all(np.array_equal(x, y) for x, y in zip(qs, b.get_q()))
+
+
+def _spin_energy_ref(qset, G, beta):
+    m = len(qset)
+    E = 0.
+    for im in range(m):
+        E += np.sum(qset[im].astype(np.float64) * qset[(im + 1) % m])
+    return E * 1. / (2 * beta) * np.log(1 / np.tanh(G * beta / m))
+
+
+def test_get_system_E(sq):
+    G, beta = 0.01, 1. / 0.05
+    N, m = 10, 5
+    rng = np.random.default_rng(4)
+    a = sq.cuda.dense_graph_annealer(rand_sym(rng, N), n_trotters=m, algorithm=sq.algorithm.sa_default)
+    a.prepare()
+    qset = (2 * rng.integers(0, 2, (m, N)) - 1).astype(np.int8)
+    a.set_qset(qset)
+    assert np.allclose(a.get_system_E(G, beta), np.mean(a.get_E()), atol=1e-5)
+    a = sq.cuda.dense_graph_annealer(np.ones((N, N), np.float32), n_trotters=m)
+    a.prepare()
+    for sign in (1, -1):
+        a.set_q(sign * np.ones(N, np.int8))
+        ref = np.mean(a.get_E()) + _spin_energy_ref(a.get_q(), G, beta)
+        assert np.allclose(a.get_system_E(G, beta), ref, rtol=1e-5, atol=1e-4)
+
+
+# -------------------------------------------------------- brute force
+@pytest.mark.parametrize("name", ["int12", "int16", "int16max", "ex8", "pos8min", "neg8min", "pos8max", "r10"])
+def test_dense_bf_golden(sq, golden, name):
+    W = golden["bf_%s_W" % name].astype(np.float32)
+    om = sq.maximize if int(golden["bf_%s_om" % name]) else sq.minimize
+    s = sq.cuda.dense_graph_bf_searcher(W, om)
+    s.search()
+    E, x = s.get_E(), np.array(s.get_x())
+    assert np.allclose(E, golden["bf_%s_E" % name][0], atol=1e-6)
+    assert np.array_equal(x, golden["bf_%s_x" % name])
+
+
+def test_dense_bf_minimum_run_vs_cpu_reference(sq, orc, golden):
+    """sqaodc/tests/CUDADenseGraphBFSolverTest.cpp:218-247 at N = 16, and integer
+    W uniform in [-8, 8] at N = 20: Emin and argmin set bit-exact."""
+    W16 = golden["bf_int16_W"].astype(np.float32)
+    rng = np.random.default_rng(0)
+    U = rng.integers(-8, 9, (20, 20))
+    W20 = (np.triu(U) + np.triu(U, 1).T).astype(np.float32)
+    for W in (W16, W20):
+        E_ref, xs_ref = orc.dg_bf_search_ref(W, n_workers=0)
+        s = sq.cuda.dense_graph_bf_searcher(W)
+        s.search()
+        assert s.get_E()[0] == E_ref
+        assert np.array_equal(np.array(s.get_x()), orc.unpack_bits(xs_ref, W.shape[0]))
+
+
+def test_dense_bf_search_range_tiles(sq, orc):
+    """search_range over small tiles == search(), including ties and the tile cap."""
+    rng = np.random.default_rng(9)
+    U = rng.integers(-1, 2, (14, 14))
+    W = (np.triu(U) + np.triu(U, 1).T).astype(np.float32)
+    s1 = sq.cuda.dense_graph_bf_searcher(W, tile_size=256)
+    s1.search()
+    s2 = sq.cuda.dense_graph_bf_searcher(W, tile_size=256)
+    s2.prepare()
+    n = 0
+    while not s2.search_range():
+        n += 1
+    s2.make_solution()
+    assert n == (1 << 14) // 256 - 1
+    assert np.array_equal(np.array(s1.get_x()), np.array(s2.get_x()))
+    E_ref, xs_ref = orc.dg_bf_search_range(W, 0, 0, 1 << 14, 256)
+    assert s1.get_E()[0] == E_ref
+    assert np.array_equal(np.array(s1.get_x()), orc.unpack_bits(xs_ref, 14))
+    # all-zero W: every state ties; the first tile_size states are returned
+    z = sq.cuda.dense_graph_bf_searcher(np.zeros((12, 12), np.float32), tile_size=512)
+    z.search()
+    assert len(z.get_x()) == 512
+    assert np.array_equal(np.array(z.get_x()), orc.unpack_bits(np.arange(512), 12))
+
+
+def test_bipartite_bf_golden(sq, orc, golden):
+    g = golden
+    s = sq.cuda.bipartite_graph_bf_searcher(g["bbf_b0"], g["bbf_b1"], g["bbf_W"])
+    s.search()
+    assert np.allclose(s.get_E()[0], g["bbf_E"][0], atol=1e-6)
+    xs = s.get_x()
+    assert np.array_equal(np.array([p[0] for p in xs]), g["bbf_x0"])
+    assert np.array_equal(np.array([p[1] for p in xs]), g["bbf_x1"])
+    # integer problem with ties, against the reference CPU searcher
+    rng = np.random.default_rng(6)
+    b0 = rng.integers(-2, 3, 9).astype(np.float32)
+    b1 = rng.integers(-2, 3, 7).astype(np.float32)
+    W = rng.integers(-2, 3, (7, 9)).astype(np.float32)
+    E_ref, pairs = orc.bg_bf_search_sorted(b0, b1, W)
+    s = sq.cuda.bipartite_graph_bf_searcher(b0, b1, W, tile_size_0=256, tile_size_1=256)
+    s.search()
+    got = sorted((bits_to_int(p[0]), bits_to_int(p[1])) for p in s.get_x())
+    assert s.get_E()[0] == E_ref
+    assert got == sorted((int(a), int(b)) for a, b in pairs)
+    s2 = sq.cuda.bipartite_graph_bf_searcher(b0, b1, W, tile_size_0=256, tile_size_1=256)
+    s2.prepare()
+    while not s2.search_range():
+        pass
+    s2.make_solution()
+    assert [(tuple(a), tuple(b)) for a, b in s2.get_x()] == [(tuple(a), tuple(b)) for a, b in s.get_x()]
+
+
+def test_bf_known_answers(sq):
+    N = 8
+    for W, om, E, x in ((np.ones((N, N)), sq.minimize, 0., 0), (-np.ones((N, N)), sq.minimize, -64., 1),
+                        (np.ones((N, N)), sq.maximize, 64., 1), (-np.ones((N, N)), sq.maximize, 0., 0)):
+        s = sq.cuda.dense_graph_bf_searcher(W.astype(np.float32), om)
+        s.search()
+        assert s.get_E()[0] == E and np.all(np.array(s.get_x()) == x)
+    s = sq.cuda.dense_graph_bf_searcher(np.ones((4, 4), np.float32), sq.maximize)
+    s.prepare()
+    s.search()
+    assert len(s.get_E()) == 1 and s.get_E()[0] == 16
