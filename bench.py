@@ -130,7 +130,8 @@ class DenseTask(ctypes.Structure):
                 ("beta", ctypes.c_void_p), ("Gs", ctypes.c_float), ("betas", ctypes.c_float),
                 ("status", ctypes.c_void_p), ("seed", ctypes.c_uint64), ("step0", ctypes.c_uint32),
                 ("N", ctypes.c_int), ("m", ctypes.c_int), ("ldJ", ctypes.c_int), ("algo", ctypes.c_int),
-                ("nSteps", ctypes.c_int)]
+                ("nSteps", ctypes.c_int), ("ws", ctypes.c_void_p), ("wsBytes", ctypes.c_ulonglong),
+                ("flags", ctypes.c_int)]
 
 
 def cpu_reference(W, steps, seed=0):
@@ -224,10 +225,17 @@ def main():
     K, Wm = args.steps, args.warmup
     idx = np.linspace(0, len(sched) - 1, max(K, 1)).round().astype(int)
 
+    L.sq103_dense_ws_bytes.restype = ctypes.c_ulonglong
+    ws_bytes = int(L.sq103_dense_ws_bytes(N, m, 1))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    multi = bool(L.sq103_dense_multicta_ok(N, m, 1))
+
     def launch(G, step):
         t = DenseTask(J=dJ.data_ptr(), h=dh.data_ptr(), q=q.data_ptr(), F=F.data_ptr(), trace=None,
-                      accepted=acc.data_ptr(), G=None, beta=None, Gs=G, betas=BETA, status=None, seed=seed,
-                      step0=step, N=N, m=m, ldJ=N, algo=1, nSteps=1)
+                      accepted=acc.data_ptr(), G=None, beta=None, Gs=G, betas=BETA, status=status.data_ptr(),
+                      seed=seed, step0=step, N=N, m=m, ldJ=N, algo=1, nSteps=1, ws=ws.data_ptr(),
+                      wsBytes=ws_bytes, flags=0)
         rc = L.sq103_dense_anneal(ctypes.byref(t), sp)
         if rc != 0:
             raise RuntimeError("sq103_dense_anneal failed: %d" % rc)
@@ -255,6 +263,8 @@ def main():
             acc_hist[i + 1].copy_(acc[0])
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
+    if int(status.item()) != 0:
+        raise RuntimeError("sweep kernel reported device status %d" % int(status.item()))
     kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = float(sum(kernel_ms))
     if dist:
@@ -304,6 +314,7 @@ def main():
                 "config": {"workload": "dense SQA coloring N=4096 m=256 beta=50 G=5*0.99^k (619-step "
                                        "schedule sampled evenly over the timed steps)",
                            "N": N, "m": m, "algorithm": "coloring", "l2": "flushed between timed steps (512 MB write)",
+                           "kernel": "one CTA per trotter (cooperative)" if multi else "one CTA per instance",
                            "parallelism": "replicas" if world > 1 else "single instance"},
                 "e2e": e2e, "gpu_launches": K,
                 "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",

@@ -78,7 +78,15 @@ typedef struct sq103_dense_task {
     int N, m, ldJ;
     int algo;             /* 0 naive, 1 coloring, 2 sa_naive */
     int nSteps;
+    void *ws;             /* optional device workspace for the multi-CTA sweep */
+    unsigned long long wsBytes; /* its size; sq103_dense_ws_bytes(N, m, nSteps) */
+    int flags;            /* 0 = choose the kernel, 1 = one CTA per instance, 2 = one CTA per trotter */
 } sq103_dense_task;
+
+/* workspace the multi-CTA sweep needs for nSteps steps (accept logs, progress words) */
+SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps);
+/* 1 if the one-CTA-per-trotter sweep can run this shape on the current device */
+SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
 
 /* QUBO -> Ising (h, J, c); replaces DeviceDenseGraphFormulas::calculateHamiltonian
  * (sqaodc/cuda/DeviceFormulas.cpp:24-31).  scratch: N doubles. */
@@ -198,6 +206,8 @@ SQ103_API int sq103_dg_annealer_get_E64(void *handle, double *E, int cap, int *n
 SQ103_API int sq103_dg_annealer_get_accepted(void *handle, unsigned long long *accepted);
 SQ103_API int sq103_dg_annealer_get_rng_state(void *handle, unsigned long long *seed, uint32_t *step);
 SQ103_API int sq103_dg_annealer_set_trace(void *handle, int enable);
+/* kernel selection for the sweep: 0 = automatic, 1 = one CTA per instance, 2 = one CTA per trotter */
+SQ103_API int sq103_dg_annealer_set_kernel(void *handle, int flags);
 SQ103_API int sq103_dg_annealer_get_trace(void *handle, uint32_t *bits, int nwords);
 
 SQ103_API int sq103_bg_annealer_new(void **handle);

@@ -208,13 +208,21 @@ __global__ void randomize_kernel(int8_t *q, int N, int m, uint64_t seed, uint32_
 
 static int g_max_smem = -1;
 
+// largest dynamic shared memory the CTA kernel may use (opt-in limit minus its
+// static shared memory); sets the kernel attribute once per process
 static int max_dyn_smem() {
     if (g_max_smem < 0) {
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        g_max_smem = v;
-        cudaFuncSetAttribute(dense_sweep_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+        cudaFuncAttributes fa;
+        cudaFuncGetAttributes(&fa, dense_sweep_cta);
+        int dyn = v - (int)fa.sharedSizeBytes;
+        if (cudaFuncSetAttribute(dense_sweep_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) {
+            cudaGetLastError();
+            dyn = 48 * 1024 - (int)fa.sharedSizeBytes;
+        }
+        g_max_smem = dyn;
     }
     return g_max_smem;
 }
@@ -222,7 +230,7 @@ static int max_dyn_smem() {
 static size_t cta_smem_bytes(int N, int m) {
     size_t base = ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
     size_t stage = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
-    size_t lim = (size_t)max_dyn_smem() - 1024;  // static shared memory headroom
+    size_t lim = (size_t)max_dyn_smem();
     if (base + stage <= lim) return base + stage;
     return base;
 }
@@ -243,9 +251,20 @@ SQ103_API int sq103_randomize_spins(int8_t *q, int N, int m, uint64_t seed, uint
     return (int)cudaGetLastError();
 }
 
+int sq103_dense_anneal_multi(const sq103_dense_task *t, void *stream);
+
 SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
     if (!task || task->N <= 0 || task->m <= 0 || task->nSteps < 0) return kErrBadShape;
     if (task->nSteps == 0) return 0;
+    // one CTA per trotter when the shape allows it (or when asked to), else one CTA
+    bool multi = task->flags == 2 ||
+                 (task->flags == 0 && task->ws &&
+                  task->wsBytes >= sq103_dense_ws_bytes(task->N, task->m, task->nSteps) &&
+                  sq103_dense_multicta_ok(task->N, task->m, task->algo));
+    if (multi) {
+        if (!sq103_dense_multicta_ok(task->N, task->m, task->algo)) return kErrBadShape;
+        return sq103_dense_anneal_multi(task, stream);
+    }
     size_t smem = cta_smem_bytes(task->N, task->m);
     if (smem > (size_t)max_dyn_smem()) return kErrBadShape;  // flip lists alone do not fit
     dense_sweep_cta<<<1, kBlockThreads, smem, (cudaStream_t)stream>>>(nullptr, *task, (int)smem);

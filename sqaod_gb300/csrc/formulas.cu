@@ -11,9 +11,12 @@
 //
 // spin_gemm: C[y][n] = sum_k q[y][k] * B(k, n) with q in {-1, +1} (int8).
 // Used for the dense field refresh F = q J (J symmetric), the bipartite
-// half-step fields and the energies.  Each output is the FP64 sum, in k order,
-// of fp32 partial sums over 32-wide k chunks (the products are exact), so the
-// result is deterministic and within a few fp32 ulps of the exact sum.
+// half-step fields and the energies.  The products are exact.  fp32 outputs
+// (fields) are the FP64 sum, in k order, of fp32 partial sums over 32-wide k
+// chunks: deterministic and within a few fp32 ulps of the exact sum.  FP64
+// outputs (energies) accumulate every product in FP64.
+#include <type_traits>
+
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
@@ -113,6 +116,7 @@ __global__ void bg_hamiltonian_cols(const float *W, int N0, int N1, float sign, 
 template <bool TRANS_B, typename OutT>
 __global__ void __launch_bounds__(256) spin_gemm_kernel(const int8_t *A, int lda, const float *Bm, int ldb,
                                                         OutT *C, int ldc, int M, int Nn, int K) {
+    constexpr bool EXACT = std::is_same<OutT, double>::value;
     __shared__ float As[32][64 + 4];
     __shared__ float Bs[32][64 + 4];
     int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -148,22 +152,38 @@ __global__ void __launch_bounds__(256) spin_gemm_kernel(const int8_t *A, int lda
         for (int a = 0; a < 4; ++a)
 #pragma unroll
             for (int b = 0; b < 4; ++b) part[a][b] = 0.f;
+        if (EXACT) {
+            // energies: every (exact) product accumulated in FP64
+#pragma unroll 4
+            for (int kk = 0; kk < 32; ++kk) {
+                double av[4], bv[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) av[a] = As[kk][ty * 4 + a];
+#pragma unroll
+                for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx * 4 + b];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+            }
+        } else {
 #pragma unroll 8
-        for (int kk = 0; kk < 32; ++kk) {
-            float av[4], bv[4];
+            for (int kk = 0; kk < 32; ++kk) {
+                float av[4], bv[4];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) av[a] = As[kk][ty * 4 + a];
+                for (int a = 0; a < 4; ++a) av[a] = As[kk][ty * 4 + a];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx * 4 + b];
+                for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx * 4 + b];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) part[a][b] = __fmaf_rn(av[a], bv[b], part[a][b]);
+            }
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int b = 0; b < 4; ++b) part[a][b] = __fmaf_rn(av[a], bv[b], part[a][b]);
+                for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
         }
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] += (double)part[a][b];
         __syncthreads();
     }
 #pragma unroll

@@ -264,6 +264,7 @@ public:
 
     void calculate_E() override {
         throwErrorIfQNotSet();
+        checkStatus();
         d_r_.ensure((size_t)m_ * N_);
         SQ_CHECK(sq103_dense_energy(d_J_.p, N_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize, d_r_.p,
                                     d_E64_.p, d_E32_.p, st_.get()));
@@ -373,7 +374,9 @@ private:
         int algo = algo_ == sq::algoNaive ? kNaive : (algo_ == sq::algoSANaive ? kSANaive : kColoring);
         d_acc_.ensure(1);
         if (!accInit_) {
+            d_status_.ensure(1);
             SQ_CHECK(cudaMemsetAsync(d_acc_.p, 0, sizeof(unsigned long long), st_.get()));
+            SQ_CHECK(cudaMemsetAsync(d_status_.p, 0, sizeof(int), st_.get()));
             accInit_ = true;
         }
         size_t words = ((size_t)N_ * m_ + 31) / 32;
@@ -408,6 +411,14 @@ private:
             t.ldJ = N_;
             t.algo = algo;
             t.nSteps = chunk;
+            t.status = d_status_.p;
+            t.flags = kernelFlags_;
+            if (algo != kNaive) {
+                unsigned long long wsb = sq103_dense_ws_bytes(N_, m_, chunk);
+                d_ws_.ensure(wsb);
+                t.ws = d_ws_.p;
+                t.wsBytes = wsb;
+            }
             SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
             step_ += (uint32_t)chunk;
             stepsSinceRefresh_ += chunk;
@@ -416,9 +427,22 @@ private:
         clearState(solSolutionAvailable);
     }
 
+    // a kernel that gave up a bounded wait leaves a status word: report it at the next sync
+    void checkStatus() {
+        if (!d_status_.p) return;
+        int v = 0;
+        SQ_CHECK(cudaMemcpyAsync(&v, d_status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        if (v != 0) {
+            SQ_CHECK(cudaMemsetAsync(d_status_.p, 0, sizeof(int), st_.get()));
+            sq::throwError("annealOneStep: device wait timed out (status %d); spins are not valid.", v);
+        }
+    }
+
     void syncBits() {
         size_t mn = (size_t)m_ * N_;
         h_q_.ensure(mn);
+        checkStatus();
         SQ_CHECK(cudaMemcpyAsync(h_q_.p, d_q_.p, mn, cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
         qlist_.clear();
@@ -446,6 +470,15 @@ private:
     uint32_t step_ = 0;
     bool trace_ = false, accInit_ = false;
     int refreshPeriod_ = 8, stepsSinceRefresh_ = 0;
+    int kernelFlags_ = 0;
+    DevBuf<unsigned char> d_ws_;
+    DevBuf<int> d_status_;
+
+public:
+    void setKernel(int flags) {
+        throwErrorIf(flags < 0 || flags > 2, "kernel selector must be 0 (auto), 1 (one CTA) or 2 (CTA per trotter).");
+        kernelFlags_ = flags;
+    }
 };
 
 // =================================================== bipartite annealer

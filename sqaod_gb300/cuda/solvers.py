@@ -215,6 +215,10 @@ class DenseGraphAnnealer(_Handle):
         self._call('get_trace', ptr(out), _c_int(nwords))
         return out
 
+    def set_kernel(self, flags):
+        """Sweep kernel: 0 automatic, 1 one CTA per instance, 2 one CTA per trotter (extension)."""
+        self._call('set_kernel', _c_int(flags))
+
 
 class BipartiteGraphAnnealer(_Handle):
     """Bipartite-graph annealer (sqaodpy/sqaod/common/bipartite_graph_annealer_base.py)."""

@@ -83,8 +83,11 @@ def test_dense_energy_vs_fp64_large(sq, orc):
     a.randomize_spin()
     q = np.array(a.get_q())
     h, J, c = orc.dg_hamiltonian(W)
-    assert rel_close(a.get_E64(), orc.dg_energy_ising(h, J, c, q), 1e-9)
+    # spec criterion: within 1e-5 of the all-FP64 oracle
     assert rel_close(a.get_E(), orc.dg_energy_ising(h, J, c, q))
+    # the FP64 evaluation itself: exact up to rounding, given the fp32 h and J the API stores
+    h32, J32, _ = a.get_hamiltonian()
+    assert rel_close(a.get_E64(), orc.dg_energy_ising(h32, J32, c, q), 1e-11)
 
 
 def test_known_energies(sq):
@@ -190,6 +193,51 @@ def test_bipartite_sweep_replays_fp64(sq, orc, algo, N0, N1, m):
         q0 = np.array([p[0] for p in pairs])
         q1 = np.array([p[1] for p in pairs])
         assert np.array_equal(q0, r0) and np.array_equal(q1, r1)
+        assert st["n_mismatch"] == st["n_mismatch_small"], st
+
+
+@pytest.mark.parametrize("algo", ["coloring", "sa_naive"])
+@pytest.mark.parametrize("N,m", [(128, 16), (256, 7), (96, 2), (512, 64)])
+def test_dense_multi_cta_equals_single_cta(sq, algo, N, m):
+    """One CTA per trotter (cooperative) and one CTA per instance run the same
+    trials with the same fp32 arithmetic: spins and FP64 energies bit-identical."""
+    rng = np.random.default_rng(N + m)
+    W = rand_sym(rng, N)
+    G = [5.0 * 0.9 ** k for k in range(12)]
+    out = []
+    for flags in (1, 2):
+        a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm=algo)
+        a.set_kernel(flags)
+        a.seed(21)
+        a.prepare()
+        a.randomize_spin()
+        a.anneal(np.array(G, np.float32), 20.0)
+        out.append((np.array(a.get_q()), a.get_E64(), a.get_accepted()))
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("algo", ["coloring", "sa_naive"])
+def test_dense_multi_cta_replays_fp64(sq, orc, algo):
+    N, m = 160, 9
+    rng = np.random.default_rng(77)
+    W = rand_sym(rng, N)
+    a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm=algo)
+    a.set_kernel(2)
+    a.seed(5)
+    a.prepare()
+    a.randomize_spin()
+    q = np.array(a.get_q())
+    h, J, c = a.get_hamiltonian()
+    a.set_trace(True)
+    for G, beta in [(2.0, 10.0), (0.2, 30.0), (0.02, 50.0)]:
+        _, step = a.get_rng_state()
+        a.anneal_one_step(G, beta)
+        trace = a.get_trace((N * m + 31) // 32)
+        q_host, st = orc.dg_replay(h, J, m, DENSE_ALGOS[algo], 5, step, G, beta, q, trace, MARGIN_TOL)
+        q = np.array(a.get_q())
+        assert np.array_equal(q, q_host)
         assert st["n_mismatch"] == st["n_mismatch_small"], st
 
 
