@@ -25,6 +25,8 @@
 // bounded (global timer) and ends the kernel with a timeout status instead of
 // hanging.  Before waiting a CTA publishes its own progress, so waits always
 // point to strictly earlier trials and cannot form a cycle.
+#include <cooperative_groups.h>
+
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
@@ -106,7 +108,9 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
         S.done = 0;
         S.nflip = 0;
     }
-    __syncthreads();
+    // every CTA has read its neighbours' rows before any CTA can finish and
+    // write its own row back
+    cooperative_groups::this_grid().sync();
 
     if (warp == 0) {
         // ------------------------------------------------------------ decider
