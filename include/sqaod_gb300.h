@@ -111,6 +111,18 @@ SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream);
 /* nTasks instances in one launch; d_tasks lives in device memory. */
 SQ103_API int sq103_dense_anneal_batch(const sq103_dense_task *d_tasks, int nTasks, int maxN, int maxM,
                                        void *stream);
+/* Persistent batch sweep: `grid` CTAs take instances from d_queue (two ints,
+ * zero before the first launch; the kernel leaves them zero) in the order
+ * d_order (largest first); instance i runs steps [d_pos[i], d_pos[i] +
+ * stepsPerLaunch) of its schedule (task.nSteps steps in total, task.G /
+ * task.beta indexed by step) and advances d_pos[i].  Replaying the same
+ * launch (e.g. from a CUDA graph) therefore advances every instance.
+ * smemBytes: shared memory per CTA (instances whose spins and fields fit are
+ * staged there). */
+SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_order, int *d_pos,
+                                       int *d_queue, int stepsPerLaunch, int grid, int smemBytes, void *stream);
+SQ103_API int sq103_dense_batch_max_smem(void);
+SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes);
 
 /* -------------------------------------------- kernel layer: bipartite */
 
@@ -275,6 +287,25 @@ SQ103_API int sq103_bg_bf_make_solution(void *handle);
 SQ103_API int sq103_bg_bf_search_range(void *handle, unsigned long long *curX0, unsigned long long *curX1,
                                        int *done);
 SQ103_API int sq103_bg_bf_search(void *handle);
+
+/* ------------------------------------- handle layer: batched annealer */
+/* Many independent dense instances annealed in lock-step, one persistent
+ * launch per step (replayed from a CUDA graph when useGraph != 0).  No
+ * counterpart method table in the reference; each instance follows exactly
+ * the rules of sq103_dg_annealer (same seed -> same result).  Coloring
+ * algorithm (SA when m == 1). */
+SQ103_API int sq103_dense_batch_new(void **handle);
+SQ103_API int sq103_dense_batch_delete(void *handle);
+SQ103_API int sq103_dense_batch_add(void *handle, const float *W, int N, int m, int optimize,
+                                    unsigned long long seed, int *index);
+SQ103_API int sq103_dense_batch_set_schedule(void *handle, const float *G, const float *beta, int nSteps);
+SQ103_API int sq103_dense_batch_prepare(void *handle);
+SQ103_API int sq103_dense_batch_autotune(void *handle, int trialSteps, int *smemBytes);
+SQ103_API int sq103_dense_batch_anneal(void *handle, int nSteps, int useGraph);
+SQ103_API int sq103_dense_batch_sync(void *handle);
+SQ103_API int sq103_dense_batch_info(void *handle, int *nInst, int *pos, int *grid, int *smemBytes);
+SQ103_API int sq103_dense_batch_get_E(void *handle, int index, double *E, int cap, int *n);
+SQ103_API int sq103_dense_batch_get_q(void *handle, int index, int8_t *q, int capRows, int *m);
 
 #ifdef __cplusplus
 }

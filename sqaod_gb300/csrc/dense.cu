@@ -57,12 +57,10 @@ __device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F,
     }
 }
 
-// One CTA anneals one instance (all trotters).  Spins, fields and h are staged
-// in shared memory when they fit; otherwise the CTA works on global memory.
-__global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_dense_task *tasks,
-                                                                 sq103_dense_task single, int smemBytes) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const sq103_dense_task T = tasks ? tasks[blockIdx.x] : single;
+// One CTA anneals one instance (all trotters) for steps [s0, s0 + nSteps) of
+// its schedule.  Spins, fields and h are staged in shared memory when they
+// fit; otherwise the CTA works on global memory.
+__device__ void anneal_instance(const sq103_dense_task &T, unsigned char *smem, int smemBytes, int s0, int nSteps) {
     const int N = T.N, m = T.m, tid = threadIdx.x;
     Flip *flips = reinterpret_cast<Flip *>(smem);            // 2 x m
     int *nflip = reinterpret_cast<int *>(flips + 2 * m);      // 2 counters
@@ -95,11 +93,11 @@ __global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_den
     __shared__ Flip naiveFlip;
     __shared__ int naiveAcc;
 
-    for (int s = 0; s < T.nSteps; ++s) {
+    for (int s = s0; s < s0 + nSteps; ++s) {
         const float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
         const StepConst sc = step_const(T.algo, m, G, beta);
         const uint32_t step = T.step0 + (uint32_t)s;
-        uint32_t *trace = T.trace ? T.trace + (size_t)s * wordsPerStep : nullptr;
+        uint32_t *trace = T.trace ? T.trace + (size_t)(s - s0) * wordsPerStep : nullptr;
 
         if (T.algo == kNaive) {
             const long long nTrials = (long long)N * m;
@@ -192,6 +190,48 @@ __global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_den
             T.q[i] = q[i];
         }
     }
+    __syncthreads();  // shared memory is reused by the CTA's next instance
+}
+
+__global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_dense_task *tasks,
+                                                                 sq103_dense_task single, int smemBytes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const sq103_dense_task T = tasks ? tasks[blockIdx.x] : single;
+    anneal_instance(T, smem, smemBytes, 0, T.nSteps);
+}
+
+// Persistent batch: CTAs take instances from a queue (order[] lists them
+// largest first); instance i runs steps [pos[i], pos[i] + stepsPerLaunch) of
+// its own schedule (T.nSteps steps in total) and advances pos[i], so the same
+// launch replayed from a CUDA graph moves every instance one step further.
+__global__ void __launch_bounds__(kBlockThreads) dense_batch_persistent(const sq103_dense_task *tasks, int nTasks,
+                                                                        const int *order, int *pos, int *queue,
+                                                                        int stepsPerLaunch, int smemBytes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int item;
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int idx = item;
+        __syncthreads();
+        if (idx >= nTasks) break;
+        const int ti = order ? order[idx] : idx;
+        const sq103_dense_task T = tasks[ti];
+        const int s0 = pos[ti];
+        const int n = min(stepsPerLaunch, T.nSteps - s0);
+        if (n > 0) {
+            anneal_instance(T, smem, smemBytes, s0, n);
+            if (threadIdx.x == 0) pos[ti] = s0 + n;
+        }
+    }
+    // the last CTA to leave resets the queue for the next replay
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+        }
+    }
 }
 
 __global__ void randomize_kernel(int8_t *q, int N, int m, uint64_t seed, uint32_t step, uint32_t tag) {
@@ -268,6 +308,36 @@ SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
     size_t smem = cta_smem_bytes(task->N, task->m);
     if (smem > (size_t)max_dyn_smem()) return kErrBadShape;  // flip lists alone do not fit
     dense_sweep_cta<<<1, kBlockThreads, smem, (cudaStream_t)stream>>>(nullptr, *task, (int)smem);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_batch_max_smem(void) { return max_dyn_smem(); }
+
+SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes) {
+    int perSm = 0;
+    max_dyn_smem();
+    cudaFuncSetAttribute(dense_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_batch_persistent, kBlockThreads, smemBytes) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return perSm;
+}
+
+SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_order, int *d_pos,
+                                       int *d_queue, int stepsPerLaunch, int grid, int smemBytes, void *stream) {
+    if (nTasks <= 0) return 0;
+    if (grid <= 0 || smemBytes < 0 || smemBytes > max_dyn_smem()) return kErrBadShape;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e =
+            cudaFuncSetAttribute(dense_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
+        if (e != cudaSuccess) return (int)e;
+        attr = true;
+    }
+    dense_batch_persistent<<<grid, kBlockThreads, smemBytes, (cudaStream_t)stream>>>(
+        d_tasks, nTasks, d_order, d_pos, d_queue, stepsPerLaunch, smemBytes);
     return (int)cudaGetLastError();
 }
 

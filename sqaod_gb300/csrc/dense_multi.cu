@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
 
             unsigned accBits = 0;
             int nf = 0;
-            bool flushed = false;
+            int published = g0;  // iterations [0, published) are visible to the neighbours
             for (int i = 0; i < nValid; ++i) {
                 const int xi = __shfl_sync(FULL, x, i);
                 const int gi = g0 + i;
@@ -194,12 +194,12 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
                             ready = jc < 0;
                         }
                         if (ready) break;
-                        if (!flushed) {  // publish what is decided before waiting
+                        if (published < gi) {  // publish everything decided before waiting
                             if (lane == 0) {
                                 __stcg(outLog + (size_t)y * nWords + (g0 >> 5), accBits);
                                 st_release_gpu(progress + (size_t)y * kProgStride, (unsigned)gi);
                             }
-                            flushed = true;
+                            published = gi;
                         }
                         if (tStart == 0) tStart = global_ns();
                         if (global_ns() - tStart > kWaitLimitNs) {

@@ -21,6 +21,7 @@
 #include <time.h>
 
 #include <algorithm>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -1166,6 +1167,260 @@ private:
     float slack_ = 0.f;
     sq::BitSetPairArray xList_;
     Vector E_;
+};
+
+// ===================================================== batched annealer
+// Many independent dense instances annealed together: every annealOneStep of
+// all of them is one persistent launch (sq103_dense_batch_launch) replayed
+// from a CUDA graph.  Each instance follows exactly the rules of the
+// single-instance annealer (same Philox stream for the same seed, same field
+// refresh every kRefreshPeriod steps), so its result is bit-identical to
+// annealing it alone.
+class DenseBatch : public sq::NullBase {
+public:
+    static constexpr int kRefreshPeriod = 8;
+
+    struct Inst {
+        int N, m;
+        unsigned long long seed;
+        DevBuf<unsigned char> mem;
+        float *J, *h, *c32, *F;
+        double *c64;
+        int8_t *q;
+    };
+
+    ~DenseBatch() {
+        if (graph_) cudaGraphExecDestroy(graph_);
+    }
+
+    int add(const float *W, int N, int m, int optimize, unsigned long long seed) {
+        throwErrorIf(prepared_, "instances must be added before prepare().");
+        throwErrorIf(N <= 0 || m <= 0, "N and m must be positive.");
+        for (int r = 0; r < N; ++r)
+            for (int c = 0; c < r; ++c)
+                throwErrorIf(W[(size_t)r * N + c] != W[(size_t)c * N + r], "%s, Matrix is not symmetric.", __func__);
+        insts_.emplace_back(new Inst());
+        Inst &in = *insts_.back();
+        in.N = N;
+        in.m = m;
+        in.seed = seed;
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        size_t oJ = 0, oh = oJ + al((size_t)N * N * 4), oc = oh + al((size_t)N * 4), oc64 = oc + 256,
+               oF = oc64 + 256, oq = oF + al((size_t)m * N * 4), total = oq + al((size_t)m * N);
+        in.mem.ensure(total);
+        unsigned char *b = in.mem.p;
+        in.J = (float *)(b + oJ);
+        in.h = (float *)(b + oh);
+        in.c32 = (float *)(b + oc);
+        in.c64 = (double *)(b + oc64);
+        in.F = (float *)(b + oF);
+        in.q = (int8_t *)(b + oq);
+        dW_.ensure((size_t)N * N);
+        scratch_.ensure(N);
+        SQ_CHECK(cudaMemcpyAsync(dW_.p, W, sizeof(float) * N * N, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, optimize, in.h, in.J, N, in.c32, in.c64, scratch_.p, st_.get()));
+        st_.sync();
+        optimize_.push_back(optimize);
+        return (int)insts_.size() - 1;
+    }
+
+    void setSchedule(const float *G, const float *beta, int nSteps) {
+        throwErrorIf(nSteps <= 0, "schedule must have at least one step.");
+        sched_.ensure(2 * (size_t)nSteps);
+        SQ_CHECK(cudaMemcpyAsync(sched_.p, G, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(sched_.p + nSteps, beta, sizeof(float) * nSteps, cudaMemcpyHostToDevice, st_.get()));
+        nSched_ = nSteps;
+        st_.sync();
+        prepared_ = false;
+    }
+
+    // randomize every instance (Philox step 0 of its seed), refresh fields, upload tasks
+    void prepare() {
+        throwErrorIf(insts_.empty(), "no instance added.");
+        throwErrorIf(nSched_ <= 0, "set a schedule before prepare().");
+        const int n = (int)insts_.size();
+        std::vector<sq103_dense_task> tasks(n);
+        int maxN = 0, maxM = 0;
+        for (int i = 0; i < n; ++i) {
+            Inst &in = *insts_[i];
+            SQ_CHECK(sq103_randomize_spins(in.q, in.N, in.m, in.seed, 0, 0, st_.get()));
+            SQ_CHECK(sq103_dense_field_refresh(in.J, in.N, in.q, in.F, in.N, in.m, st_.get()));
+            sq103_dense_task t = {};
+            t.J = in.J;
+            t.h = in.h;
+            t.q = in.q;
+            t.F = in.F;
+            t.accepted = nullptr;
+            t.G = sched_.p;
+            t.beta = sched_.p + nSched_;
+            t.seed = in.seed;
+            t.step0 = 1;  // step 0 of the Philox counter is the randomisation
+            t.N = in.N;
+            t.m = in.m;
+            t.ldJ = in.N;
+            t.algo = in.m == 1 ? kSANaive : kColoring;
+            t.nSteps = nSched_;
+            tasks[i] = t;
+            maxN = std::max(maxN, in.N);
+            maxM = std::max(maxM, in.m);
+        }
+        // largest instances first: the queue then balances the tail
+        std::vector<int> order(n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return (long long)insts_[a]->N * insts_[a]->m > (long long)insts_[b]->N * insts_[b]->m;
+        });
+        dTasks_.ensure(n);
+        dOrder_.ensure(n);
+        dPos_.ensure(n);
+        dQueue_.ensure(2);
+        SQ_CHECK(cudaMemcpyAsync(dTasks_.p, tasks.data(), sizeof(sq103_dense_task) * n, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(dOrder_.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(dQueue_.p, 0, sizeof(int) * 2, st_.get()));
+        st_.sync();
+        pos_ = 0;
+        if (smem_ < 0) chooseConfig(-1);
+        if (graph_) {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+        prepared_ = true;
+    }
+
+    // the launch configuration (shared memory per CTA -> CTAs per SM) only
+    // changes speed, never results
+    void chooseConfig(int smemBytes) {
+        int dev = 0, sms = 0;
+        SQ_CHECK(cudaGetDevice(&dev));
+        SQ_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int maxS = sq103_dense_batch_max_smem();
+        smem_ = smemBytes < 0 ? std::min(maxS, 96 * 1024) : std::min(smemBytes, maxS);
+        int per = std::max(1, sq103_dense_batch_ctas_per_sm(smem_));
+        grid_ = std::max(1, std::min((int)insts_.size(), per * sms));
+        if (graph_) {
+            cudaGraphExecDestroy(graph_);
+            graph_ = nullptr;
+        }
+    }
+
+    // times a few candidate configurations on copies of the instance state and keeps the fastest
+    int autotune(int trialSteps) {
+        throwErrorIf(!prepared_, "prepare() first.");
+        const int n = (int)insts_.size();
+        std::vector<DevBuf<unsigned char>> saveQ(n), saveF(n);
+        for (int i = 0; i < n; ++i) {
+            Inst &in = *insts_[i];
+            saveQ[i].ensure((size_t)in.m * in.N);
+            saveF[i].ensure((size_t)in.m * in.N * 4);
+            SQ_CHECK(cudaMemcpyAsync(saveQ[i].p, in.q, (size_t)in.m * in.N, cudaMemcpyDeviceToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(saveF[i].p, in.F, (size_t)in.m * in.N * 4, cudaMemcpyDeviceToDevice, st_.get()));
+        }
+        int maxS = sq103_dense_batch_max_smem();
+        int cands[] = {0, 24 * 1024, 48 * 1024, 96 * 1024, maxS};
+        float best = 1e30f;
+        int bestS = smem_;
+        cudaEvent_t e0, e1;
+        SQ_CHECK(cudaEventCreate(&e0));
+        SQ_CHECK(cudaEventCreate(&e1));
+        for (int c : cands) {
+            if (c > maxS) continue;
+            chooseConfig(c);
+            SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+            SQ_CHECK(cudaEventRecord(e0, st_.get()));
+            for (int s = 0; s < trialSteps; ++s) launchOne();
+            SQ_CHECK(cudaEventRecord(e1, st_.get()));
+            SQ_CHECK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            SQ_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bestS = c;
+            }
+            for (int i = 0; i < n; ++i) {  // restore the state
+                Inst &in = *insts_[i];
+                SQ_CHECK(cudaMemcpyAsync(in.q, saveQ[i].p, (size_t)in.m * in.N, cudaMemcpyDeviceToDevice, st_.get()));
+                SQ_CHECK(cudaMemcpyAsync(in.F, saveF[i].p, (size_t)in.m * in.N * 4, cudaMemcpyDeviceToDevice, st_.get()));
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+        st_.sync();
+        chooseConfig(bestS);
+        return bestS;
+    }
+
+    // nSteps further steps of every instance (bounded by the schedule length)
+    void anneal(int nSteps, bool useGraph) {
+        throwErrorIf(!prepared_, "prepare() first.");
+        for (int s = 0; s < nSteps && pos_ < nSched_; ++s) {
+            if (pos_ > 0 && pos_ % kRefreshPeriod == 0) refreshAll();
+            if (useGraph) {
+                if (!graph_) captureStep();
+                SQ_CHECK(cudaGraphLaunch(graph_, st_.get()));
+            } else {
+                launchOne();
+            }
+            ++pos_;
+        }
+    }
+
+    void sync() { st_.sync(); }
+    int size() const { return (int)insts_.size(); }
+    int position() const { return pos_; }
+    int grid() const { return grid_; }
+    int smem() const { return smem_; }
+    const Inst &inst(int i) const {
+        throwErrorIf(i < 0 || i >= (int)insts_.size(), "instance index out of range.");
+        return *insts_[i];
+    }
+
+    void energies(int i, double *E) {
+        const Inst &in = inst(i);
+        r_.ensure((size_t)in.m * in.N);
+        E64_.ensure(in.m);
+        SQ_CHECK(sq103_dense_energy(in.J, in.N, in.h, in.c64, in.q, in.N, in.m, optimize_[i], r_.p, E64_.p, nullptr,
+                                    st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(E, E64_.p, sizeof(double) * in.m, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+    }
+
+    void spins(int i, int8_t *q) {
+        const Inst &in = inst(i);
+        SQ_CHECK(cudaMemcpyAsync(q, in.q, (size_t)in.m * in.N, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+    }
+
+private:
+    void launchOne() {
+        SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, (int)insts_.size(), dOrder_.p, dPos_.p, dQueue_.p, 1, grid_, smem_,
+                                          st_.get()));
+    }
+
+    void refreshAll() {
+        for (auto &p : insts_) SQ_CHECK(sq103_dense_field_refresh(p->J, p->N, p->q, p->F, p->N, p->m, st_.get()));
+    }
+
+    void captureStep() {
+        cudaGraph_t g;
+        SQ_CHECK(cudaStreamBeginCapture(st_.get(), cudaStreamCaptureModeThreadLocal));
+        launchOne();
+        SQ_CHECK(cudaStreamEndCapture(st_.get(), &g));
+        SQ_CHECK(cudaGraphInstantiate(&graph_, g, 0));
+        cudaGraphDestroy(g);
+    }
+
+    Stream st_;
+    std::vector<std::unique_ptr<Inst>> insts_;
+    std::vector<int> optimize_;
+    DevBuf<float> dW_, sched_;
+    DevBuf<double> scratch_, r_, E64_;
+    DevBuf<sq103_dense_task> dTasks_;
+    DevBuf<int> dOrder_, dPos_, dQueue_;
+    cudaGraphExec_t graph_ = nullptr;
+    int nSched_ = 0, pos_ = 0, grid_ = 1, smem_ = -1;
+    bool prepared_ = false;
 };
 
 }  // namespace sq103
