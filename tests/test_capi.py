@@ -23,7 +23,7 @@ def lib():
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "sqaod_gb300.h")).read()
-    return sorted(set(re.findall(r"\b(sq103_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"SQ103_API[^;(]*?\b(sq103_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol(lib):
