@@ -118,9 +118,11 @@ SQ103_API int sq103_dense_anneal_batch(const sq103_dense_task *d_tasks, int nTas
  * task.beta indexed by step) and advances d_pos[i].  Replaying the same
  * launch (e.g. from a CUDA graph) therefore advances every instance.
  * smemBytes: shared memory per CTA (instances whose spins and fields fit are
- * staged there). */
-SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_order, int *d_pos,
-                                       int *d_queue, int stepsPerLaunch, int grid, int smemBytes, void *stream);
+ * staged there).  d_nTasks (optional): the instance count read on the device,
+ * so that a captured launch stays valid while instances come and go. */
+SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_nTasks,
+                                       const int *d_order, int *d_pos, int *d_queue, int stepsPerLaunch, int grid,
+                                       int smemBytes, void *stream);
 SQ103_API int sq103_dense_batch_max_smem(void);
 SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes);
 
@@ -156,6 +158,12 @@ SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const floa
 /* nSteps annealOneStep of one bipartite instance
  * (CUDABipartiteGraphAnnealer::annealOneStepSQA/SA, :539-625) */
 SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task, void *stream);
+/* The persistent batch scheme of sq103_dense_batch_launch for bipartite
+ * instances (coloring / sa_coloring): one CTA runs both half-step field GEMMs
+ * and the colour phases of an instance; bit-identical to sq103_bipartite_anneal. */
+SQ103_API int sq103_bipartite_batch_launch(const sq103_bipartite_task *d_tasks, int nTasks, const int *d_nTasks,
+                                           const int *d_order, int *d_pos, int *d_queue, int stepsPerLaunch,
+                                           int grid, void *stream);
 
 /* ------------------------------------------------- kernel layer: BF */
 

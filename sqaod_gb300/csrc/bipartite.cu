@@ -16,10 +16,35 @@
 // sa_naive: per trotter, (N0+N1) m trials at x = hi(w0 (N0+N1)) of
 // philox((t, y, step, 0x34)) (CPUBipartiteGraphAnnealer.cpp:446-480).
 // The naive fields are a fixed-order block reduction of one J row or column.
+#include "spin_gemm.cuh"
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
 namespace sq103 {
+
+// one colour-phase trial of spin i of trotter y on the moving side; returns 1 if accepted
+__device__ __forceinline__ int bip_trial(int8_t *qA, const float *F, const float *h, int Ns, int m, int y, int i,
+                                         uint64_t seed, uint32_t step, uint32_t tag, const StepConst &sc, int algo,
+                                         uint32_t *trace, unsigned long long bitBase) {
+    u32x4 r = draw(seed, (uint32_t)i, (uint32_t)y, step, tag);
+    float u = draw_unit(r.y);
+    size_t o = (size_t)y * Ns + i;
+    float qyx = qA[o];
+    float dE;
+    if (algo == kSAColoring) {
+        dE = bip_sa_dE(qyx, h[i], F[o]);
+    } else {
+        int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
+        dE = bip_sqa_dE(qyx, h[i], F[o], qA[(size_t)yl * Ns + i], qA[(size_t)yr * Ns + i], sc.twoDivM, sc.coef);
+    }
+    if (!metropolis(dE, sc.rate, u)) return 0;
+    qA[o] = (int8_t)(-qyx);
+    if (trace) {
+        unsigned long long bit = bitBase + o;
+        atomicOr(&trace[bit >> 5], 1u << (bit & 31));
+    }
+    return 1;
+}
 
 __global__ void __launch_bounds__(256) bip_flip_phase(int8_t *qA, const float *F, const float *h, int Ns, int m,
                                                       int yb, int ys, int cnt, uint64_t seed, uint32_t step,
@@ -32,27 +57,7 @@ __global__ void __launch_bounds__(256) bip_flip_phase(int8_t *qA, const float *F
     if (active) {
         StepConst sc = step_const(algo, m, Gp ? *Gp : Gsc, bp ? *bp : bsc);
         int t = (int)(idx / Ns), i = (int)(idx - (long long)t * Ns);
-        int y = yb + t * ys;
-        u32x4 r = draw(seed, (uint32_t)i, (uint32_t)y, step, tag);
-        float u = draw_unit(r.y);
-        size_t o = (size_t)y * Ns + i;
-        float qyx = qA[o];
-        float dE;
-        if (algo == kSAColoring) {
-            dE = bip_sa_dE(qyx, h[i], F[o]);
-        } else {
-            int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
-            dE = bip_sqa_dE(qyx, h[i], F[o], qA[(size_t)yl * Ns + i], qA[(size_t)yr * Ns + i], sc.twoDivM,
-                            sc.coef);
-        }
-        if (metropolis(dE, sc.rate, u)) {
-            qA[o] = (int8_t)(-qyx);
-            acc = 1;
-            if (trace) {
-                unsigned long long bit = bitBase + o;
-                atomicOr(&trace[bit >> 5], 1u << (bit & 31));
-            }
-        }
+        acc = bip_trial(qA, F, h, Ns, m, yb + t * ys, i, seed, step, tag, sc, algo, trace, bitBase);
     }
     if (accepted) {
         unsigned ballot = __ballot_sync(0xffffffffu, acc);
@@ -140,9 +145,94 @@ __global__ void __launch_bounds__(256) bip_naive(sq103_bipartite_task T, int s) 
     if (threadIdx.x == 0 && T.accepted) atomicAdd(T.accepted, accepted);
 }
 
+// Persistent batch of bipartite instances (coloring / sa_coloring): one CTA
+// runs a whole annealOneStep of one instance -- both half-step field GEMMs
+// (the spin_gemm tiles, looped by the CTA) and the colour phases -- for steps
+// [pos[i], pos[i] + stepsPerLaunch) of its schedule.  Same arithmetic as
+// sq103_bipartite_anneal, so results are bit-identical.
+__global__ void __launch_bounds__(256) bip_batch_persistent(const sq103_bipartite_task *tasks, const int *nTasksDev,
+                                                            int nTasksHost, const int *order, int *pos, int *queue,
+                                                            int stepsPerLaunch) {
+    __shared__ int item;
+    const int nTasks = nTasksDev ? *nTasksDev : nTasksHost;
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(queue, 1);
+        __syncthreads();
+        const int idx = item;
+        __syncthreads();
+        if (idx >= nTasks) break;
+        const int ti = order ? order[idx] : idx;
+        const sq103_bipartite_task T = tasks[ti];
+        const int s0 = pos[ti];
+        const int n = min(stepsPerLaunch, T.nSteps - s0);
+        const int m = T.m, m2 = (m / 2) * 2;
+        const bool sa = T.algo == kSAColoring;
+        unsigned long long accepted = 0;
+        for (int s = s0; s < s0 + n; ++s) {
+            const StepConst sc = step_const(T.algo, m, T.G ? T.G[s] : T.Gs, T.beta ? T.beta[s] : T.betas);
+            const uint32_t step = T.step0 + (uint32_t)s;
+            for (int hs = 0; hs < 2; ++hs) {
+                const int side = hs == 0 ? 1 : 0;
+                const int Ns = side ? T.N1 : T.N0;
+                int8_t *qA = side ? T.q1 : T.q0;
+                float *F = side ? T.F1 : T.F0;
+                const float *h = side ? T.h1 : T.h0;
+                for (int ty = 0; ty < m; ty += 64)
+                    for (int tx = 0; tx < Ns; tx += 64) {
+                        if (side)
+                            spin_gemm_tile<true, float>(T.q0, T.N0, T.J, T.N0, F, T.N1, m, T.N1, T.N0, ty, tx);
+                        else
+                            spin_gemm_tile<false, float>(T.q1, T.N1, T.J, T.N0, F, T.N0, m, T.N0, T.N1, ty, tx);
+                    }
+                __syncthreads();
+                const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
+                for (int ph = 0; ph < 3; ++ph) {
+                    int yb, ys, cnt;
+                    if (sa) {
+                        if (ph) break;
+                        yb = 0; ys = 1; cnt = m;
+                    } else if (ph == 0) {
+                        yb = 0; ys = 2; cnt = m2 / 2;
+                    } else if (ph == 1) {
+                        if (!(m & 1)) continue;
+                        yb = m - 1; ys = 1; cnt = 1;
+                    } else {
+                        yb = 1; ys = 2; cnt = m2 / 2;
+                    }
+                    for (long long k = threadIdx.x; k < (long long)cnt * Ns; k += blockDim.x) {
+                        int t = (int)(k / Ns), i = (int)(k - (long long)t * Ns);
+                        accepted += bip_trial(qA, F, h, Ns, m, yb + t * ys, i, T.seed, step, tag, sc, T.algo, nullptr, 0);
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+        if (n > 0) {
+            if (T.accepted) atomicAdd(T.accepted, accepted);
+            if (threadIdx.x == 0) pos[ti] = s0 + n;
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(queue + 1, 1) == (int)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+        }
+    }
+}
+
 }  // namespace sq103
 
 using namespace sq103;
+
+extern "C" SQ103_API int sq103_bipartite_batch_launch(const sq103_bipartite_task *d_tasks, int nTasks,
+                                                      const int *d_nTasks, const int *d_order, int *d_pos,
+                                                      int *d_queue, int stepsPerLaunch, int grid, void *stream) {
+    if (grid <= 0) return kErrBadShape;
+    bip_batch_persistent<<<grid, 256, 0, (cudaStream_t)stream>>>(d_tasks, d_nTasks, nTasks, d_order, d_pos, d_queue,
+                                                                 stepsPerLaunch);
+    return (int)cudaGetLastError();
+}
 
 extern "C" SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task, void *stream) {
     if (!task) return kErrBadShape;

@@ -204,11 +204,13 @@ __global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_den
 // largest first); instance i runs steps [pos[i], pos[i] + stepsPerLaunch) of
 // its own schedule (T.nSteps steps in total) and advances pos[i], so the same
 // launch replayed from a CUDA graph moves every instance one step further.
-__global__ void __launch_bounds__(kBlockThreads) dense_batch_persistent(const sq103_dense_task *tasks, int nTasks,
+__global__ void __launch_bounds__(kBlockThreads) dense_batch_persistent(const sq103_dense_task *tasks,
+                                                                        int nTasksHost, const int *nTasksDev,
                                                                         const int *order, int *pos, int *queue,
                                                                         int stepsPerLaunch, int smemBytes) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int item;
+    const int nTasks = nTasksDev ? *nTasksDev : nTasksHost;
     for (;;) {
         if (threadIdx.x == 0) item = atomicAdd(queue, 1);
         __syncthreads();
@@ -325,9 +327,10 @@ SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes) {
     return perSm;
 }
 
-SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_order, int *d_pos,
-                                       int *d_queue, int stepsPerLaunch, int grid, int smemBytes, void *stream) {
-    if (nTasks <= 0) return 0;
+SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTasks, const int *d_nTasks,
+                                       const int *d_order, int *d_pos, int *d_queue, int stepsPerLaunch, int grid,
+                                       int smemBytes, void *stream) {
+    if (nTasks <= 0 && !d_nTasks) return 0;
     if (grid <= 0 || smemBytes < 0 || smemBytes > max_dyn_smem()) return kErrBadShape;
     static bool attr = false;
     if (!attr) {
@@ -337,7 +340,7 @@ SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTas
         attr = true;
     }
     dense_batch_persistent<<<grid, kBlockThreads, smemBytes, (cudaStream_t)stream>>>(
-        d_tasks, nTasks, d_order, d_pos, d_queue, stepsPerLaunch, smemBytes);
+        d_tasks, nTasks, d_nTasks, d_order, d_pos, d_queue, stepsPerLaunch, smemBytes);
     return (int)cudaGetLastError();
 }
 

@@ -1394,7 +1394,7 @@ public:
 
 private:
     void launchOne() {
-        SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, (int)insts_.size(), dOrder_.p, dPos_.p, dQueue_.p, 1, grid_, smem_,
+        SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, (int)insts_.size(), nullptr, dOrder_.p, dPos_.p, dQueue_.p, 1, grid_, smem_,
                                           st_.get()));
     }
 

@@ -45,5 +45,8 @@ def test_tc_field_refresh(N, m):
     err_tc = float((F_tc.double() - F64).abs().max())
     err_simt = float((F_simt.double() - F64).abs().max())
     assert not torch.isnan(F_tc).any()
-    # fp32 accumulation of exact products: a few ulps of the row magnitude
-    assert err_tc <= 2e-6 * scale * max(1.0, N / 1024), (err_tc, err_simt, scale)
+    print("N=%d m=%d  max |F - F64| / max|F64|: tcgen05 %.2e  simt %.2e" % (N, m, err_tc / scale, err_simt / scale))
+    # exact products, tensor-core fp32 accumulation: within 1e-5 of the FP64 fields
+    assert err_tc <= 1e-5 * scale, (err_tc, err_simt, scale)
+    # the SIMT GEMM (sequential fp32 FMAs over 32-wide chunks, FP64 across chunks)
+    assert err_simt <= 1e-6 * scale, (err_tc, err_simt, scale)
