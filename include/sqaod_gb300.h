@@ -315,6 +315,32 @@ SQ103_API int sq103_dense_batch_info(void *handle, int *nInst, int *pos, int *gr
 SQ103_API int sq103_dense_batch_get_E(void *handle, int index, double *E, int cap, int *n);
 SQ103_API int sq103_dense_batch_get_q(void *handle, int index, int8_t *q, int capRows, int *m);
 
+/* ------------------------------------------- handle layer: request server */
+/* Continuous batching of anneal requests of mixed size and type (no
+ * counterpart in the reference).  Requests are admitted FIFO while their
+ * device-memory footprint fits budgetBytes and a slot is free; every
+ * sq103_server_tick advances every active instance by one annealOneStep and
+ * completes the finished ones (FP64 energies, spins).  Each request ends
+ * exactly as the same seed and schedule would alone (sq103_dg_annealer /
+ * sq103_bg_annealer with prepare, randomize_spin and the schedule).
+ * States: 0 queued, 1 active, 2 done. */
+SQ103_API int sq103_server_new(void **handle, unsigned long long budgetBytes, int maxSlots);
+SQ103_API int sq103_server_delete(void *handle);
+SQ103_API int sq103_server_submit_dense(void *handle, const float *W, int N, int m, int optimize,
+                                        unsigned long long seed, const float *G, const float *beta, int nSteps,
+                                        int *id);
+SQ103_API int sq103_server_submit_bipartite(void *handle, const float *b0, const float *b1, const float *W,
+                                            int N0, int N1, int m, int optimize, unsigned long long seed,
+                                            const float *G, const float *beta, int nSteps, int *id);
+SQ103_API int sq103_server_tick(void *handle, int *completed);
+SQ103_API int sq103_server_state(void *handle, int id, int *state);
+/* E: m FP64 energies; q0 (m x N or m x N0) and q1 (m x N1, bipartite) spins;
+ * release != 0 frees the request's host record. */
+SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int *m, int8_t *q0, int8_t *q1,
+                                  long long capBytes, int release);
+SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *done,
+                                 unsigned long long *bytesInUse);
+
 #ifdef __cplusplus
 }
 #endif

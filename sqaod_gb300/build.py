@@ -17,7 +17,7 @@ OUT_DIR = os.path.join(HERE, "lib")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libsqaod_gb300.so"
 
-SOURCES = ["formulas.cu", "tc_gemm.cu", "dense.cu", "dense_multi.cu", "bipartite.cu", "bf.cu", "solvers.cu", "common_api.cpp"]
+SOURCES = ["formulas.cu", "tc_gemm.cu", "dense.cu", "dense_multi.cu", "bipartite.cu", "bf.cu", "solvers.cu", "serve.cu", "common_api.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -313,12 +313,31 @@ SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
     return (int)cudaGetLastError();
 }
 
-SQ103_API int sq103_dense_batch_max_smem(void) { return max_dyn_smem(); }
+// dynamic shared memory limit of the persistent batch kernel (opt-in limit minus
+// its own static shared memory); sets the attribute once per process
+static int batch_dyn_smem() {
+    static int lim = -1;
+    if (lim < 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa;
+        cudaFuncGetAttributes(&fa, dense_batch_persistent);
+        lim = v - (int)fa.sharedSizeBytes;
+        if (cudaFuncSetAttribute(dense_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            lim = 48 * 1024 - (int)fa.sharedSizeBytes;
+        }
+    }
+    return lim;
+}
+
+SQ103_API int sq103_dense_batch_max_smem(void) { return batch_dyn_smem(); }
 
 SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes) {
     int perSm = 0;
-    max_dyn_smem();
-    cudaFuncSetAttribute(dense_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
+    if (smemBytes > batch_dyn_smem()) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_batch_persistent, kBlockThreads, smemBytes) !=
         cudaSuccess) {
         cudaGetLastError();
@@ -331,14 +350,7 @@ SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTas
                                        const int *d_order, int *d_pos, int *d_queue, int stepsPerLaunch, int grid,
                                        int smemBytes, void *stream) {
     if (nTasks <= 0 && !d_nTasks) return 0;
-    if (grid <= 0 || smemBytes < 0 || smemBytes > max_dyn_smem()) return kErrBadShape;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(dense_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem());
-        if (e != cudaSuccess) return (int)e;
-        attr = true;
-    }
+    if (grid <= 0 || smemBytes < 0 || smemBytes > batch_dyn_smem()) return kErrBadShape;
     dense_batch_persistent<<<grid, kBlockThreads, smemBytes, (cudaStream_t)stream>>>(
         d_tasks, nTasks, d_nTasks, d_order, d_pos, d_queue, stepsPerLaunch, smemBytes);
     return (int)cudaGetLastError();

@@ -1,0 +1,449 @@
+// serve.cu -- continuous-batching request server for anneals of mixed size and type.
+//
+// Requests (dense or bipartite QUBO, own N, m, seed and G/beta schedule) are
+// admitted first-in first-out as soon as their device-memory footprint fits
+// the budget and a slot is free.  Admitted instances stay resident (couplings,
+// spins, fields; the RNG state is (seed, step) and lives in the task).  Every
+// tick advances every active instance by one annealOneStep:
+//   - dense instances whose spins and fields fit in shared memory, and every
+//     bipartite instance, in the persistent batch kernels (one launch each,
+//     instance count read on the device);
+//   - large dense instances with the one-CTA-per-trotter kernel;
+//   - dense fields are refreshed every 8 steps, as the single-instance annealer
+//     does, so each instance ends exactly as it would alone.
+// Finished instances get their FP64 energies and spins copied out, and their
+// slot and memory are released in the same tick, so a waiting request can be
+// admitted by the next tick.  No counterpart in the reference.
+#include <algorithm>
+#include <deque>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "host_util.h"
+#include "sq_common.cuh"
+#include "sq_kernels.h"
+
+namespace sq103 {
+
+namespace sq = sqaod;
+
+class Server : public sq::NullBase {
+public:
+    static constexpr int kRefreshPeriod = 8;
+    enum State { kQueued = 0, kActive = 1, kDone = 2 };
+
+    struct Request {
+        int id, kind;  // 0 dense, 1 bipartite
+        int N0, N1, m, optimize, nSteps;
+        unsigned long long seed;
+        std::vector<float> W, b0, b1, G, beta;
+        int state = kQueued;
+        // resident state
+        DevBuf<unsigned char> mem;
+        size_t bytes = 0;
+        int pos = 0;     // steps done
+        int slot = -1;   // batch slot, -1 for the per-instance kernel
+        bool large = false;
+        sq103_dense_task dt = {};
+        sq103_bipartite_task bt = {};
+        double *c64 = nullptr;
+        // results
+        std::vector<double> E;
+        std::vector<int8_t> q0, q1;
+    };
+
+    Server(unsigned long long budget, int maxSlots) : budget_(budget), maxSlots_(maxSlots) {
+        dTasks_.ensure(maxSlots);
+        bTasks_.ensure(maxSlots);
+        dPos_.ensure(maxSlots);
+        bPos_.ensure(maxSlots);
+        counts_.ensure(2);
+        queues_.ensure(4);
+        SQ_CHECK(cudaMemsetAsync(queues_.p, 0, sizeof(int) * 4, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(counts_.p, 0, sizeof(int) * 2, st_.get()));
+        int dev = 0;
+        SQ_CHECK(cudaGetDevice(&dev));
+        SQ_CHECK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+        stageSmem_ = std::min(sq103_dense_batch_max_smem(), 96 * 1024);
+        denseGrid_ = sms_ * std::max(1, sq103_dense_batch_ctas_per_sm(stageSmem_));
+        bipGrid_ = sms_ * 4;
+        st_.sync();
+    }
+
+    int submitDense(const float *W, int N, int m, int optimize, unsigned long long seed, const float *G,
+                    const float *beta, int nSteps) {
+        throwErrorIf(N <= 0 || m <= 0 || nSteps <= 0, "bad request shape.");
+        for (int r = 0; r < N; ++r)
+            for (int c = 0; c < r; ++c)
+                throwErrorIf(W[(size_t)r * N + c] != W[(size_t)c * N + r], "%s, Matrix is not symmetric.", __func__);
+        auto rq = std::make_unique<Request>();
+        rq->kind = 0;
+        rq->N0 = N;
+        rq->N1 = 0;
+        rq->W.assign(W, W + (size_t)N * N);
+        return enqueue(std::move(rq), m, optimize, seed, G, beta, nSteps);
+    }
+
+    int submitBipartite(const float *b0, const float *b1, const float *W, int N0, int N1, int m, int optimize,
+                        unsigned long long seed, const float *G, const float *beta, int nSteps) {
+        throwErrorIf(N0 <= 0 || N1 <= 0 || m <= 0 || nSteps <= 0, "bad request shape.");
+        auto rq = std::make_unique<Request>();
+        rq->kind = 1;
+        rq->N0 = N0;
+        rq->N1 = N1;
+        rq->W.assign(W, W + (size_t)N0 * N1);
+        rq->b0.assign(b0, b0 + N0);
+        rq->b1.assign(b1, b1 + N1);
+        return enqueue(std::move(rq), m, optimize, seed, G, beta, nSteps);
+    }
+
+    // one step of every active instance; returns the number of requests completed
+    int tick() {
+        admit();
+        const int nD = (int)denseSlots_.size(), nB = (int)bipSlots_.size();
+        if (nD > 0)
+            SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, nD, counts_.p, nullptr, dPos_.p, queues_.p, 1,
+                                              std::min(denseGrid_, nD), stageSmem_, st_.get()));
+        if (nB > 0)
+            SQ_CHECK(sq103_bipartite_batch_launch(bTasks_.p, nB, counts_.p + 1, nullptr, bPos_.p, queues_.p + 2, 1,
+                                                  std::min(bipGrid_, nB), st_.get()));
+        for (Request *r : large_) {
+            sq103_dense_task t = r->dt;
+            t.G = r->dt.G + r->pos;
+            t.beta = r->dt.beta + r->pos;
+            t.step0 = 1 + (uint32_t)r->pos;
+            t.nSteps = 1;
+            t.ws = ws_.p;
+            t.wsBytes = ws_.n;
+            SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
+        }
+        std::vector<Request *> finished;
+        for (auto &kv : active_) {
+            Request *r = kv.second;
+            r->pos += 1;
+            if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)
+                SQ_CHECK(sq103_dense_field_refresh(r->dt.J, r->N0, r->dt.q, r->dt.F, r->N0, r->m, st_.get()));
+            if (r->pos >= r->nSteps) finished.push_back(r);
+        }
+        for (Request *r : finished) complete(r);
+        ++ticks_;
+        return (int)finished.size();
+    }
+
+    int state(int id) const {
+        auto it = all_.find(id);
+        throwErrorIf(it == all_.end(), "unknown request id %d.", id);
+        return it->second->state;
+    }
+
+    const Request &request(int id) const {
+        auto it = all_.find(id);
+        throwErrorIf(it == all_.end(), "unknown request id %d.", id);
+        return *it->second;
+    }
+
+    void release(int id) {
+        auto it = all_.find(id);
+        throwErrorIf(it == all_.end(), "unknown request id %d.", id);
+        throwErrorIf(it->second->state != kDone, "request %d is not done.", id);
+        all_.erase(it);
+    }
+
+    void stats(int *queued, int *active, int *done, unsigned long long *bytes) const {
+        if (queued) *queued = (int)queue_.size();
+        if (active) *active = (int)active_.size();
+        if (done) *done = done_;
+        if (bytes) *bytes = used_;
+    }
+
+private:
+    int enqueue(std::unique_ptr<Request> rq, int m, int optimize, unsigned long long seed, const float *G,
+                const float *beta, int nSteps) {
+        rq->id = nextId_++;
+        rq->m = m;
+        rq->optimize = optimize ? 1 : 0;
+        rq->seed = seed;
+        rq->nSteps = nSteps;
+        rq->G.assign(G, G + nSteps);
+        rq->beta.assign(beta, beta + nSteps);
+        rq->bytes = footprint(*rq);
+        throwErrorIf(rq->bytes > budget_, "request of %llu bytes exceeds the device-memory budget of %llu bytes.",
+                     (unsigned long long)rq->bytes, budget_);
+        Request *p = rq.get();
+        all_[p->id] = std::move(rq);
+        queue_.push_back(p);
+        return p->id;
+    }
+
+    static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+    static size_t footprint(const Request &r) {
+        size_t s = 8 * 256 + al(r.nSteps * 4) * 2;
+        if (r.kind == 0) {
+            size_t N = r.N0, m = r.m;
+            s += al(N * N * 4) + al(N * 4) + al(m * N * 4) + al(m * N) + al(m * N * 8);
+        } else {
+            size_t N0 = r.N0, N1 = r.N1, m = r.m;
+            s += al(N0 * N1 * 4) + al(N0 * 4) + al(N1 * 4) + al(m * N0) + al(m * N1) + al(m * N0 * 4) +
+                 al(m * N1 * 4) + al(m * N1 * 8);
+        }
+        return s;
+    }
+
+    bool fitsStaging(const Request &r) const {
+        size_t base = ((size_t)(2 * r.m) * 12 + 8 + 15) & ~(size_t)15;
+        return base + (size_t)r.m * r.N0 * 5 + (size_t)r.N0 * 4 <= (size_t)stageSmem_;
+    }
+
+    void admit() {
+        bool changed = false;
+        while (!queue_.empty()) {
+            Request *r = queue_.front();
+            if (used_ + r->bytes > budget_) break;
+            bool large = r->kind == 0 && !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring);
+            if (!large && (int)(r->kind == 0 ? denseSlots_.size() : bipSlots_.size()) >= maxSlots_) break;
+            queue_.pop_front();
+            r->large = large;
+            setup(r);
+            used_ += r->bytes;
+            r->state = kActive;
+            active_[r->id] = r;
+            changed = true;
+        }
+        if (changed) {
+            int c[2] = {(int)denseSlots_.size(), (int)bipSlots_.size()};
+            SQ_CHECK(cudaMemcpyAsync(counts_.p, c, sizeof(c), cudaMemcpyHostToDevice, st_.get()));
+            st_.sync();  // the host array above is a temporary
+        }
+    }
+
+    void setup(Request *r) {
+        const int m = r->m, n = r->nSteps;
+        if (r->kind == 0) {
+            const size_t N = r->N0;
+            size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * N * 4), oc = oh + al(N * 4),
+                   oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), tot = oR + al(m * N * 8);
+            r->mem.ensure(tot);
+            unsigned char *b = r->mem.p;
+            float *G = (float *)(b + oG), *beta = (float *)(b + oB), *J = (float *)(b + oJ), *h = (float *)(b + oh);
+            float *c32 = (float *)(b + oc);
+            r->c64 = (double *)(b + oc + 256);
+            float *F = (float *)(b + oF);
+            int8_t *q = (int8_t *)(b + oq);
+            double *scratch = (double *)(b + oR);  // N doubles for the hamiltonian, m N for energies
+            SQ_CHECK(cudaMemcpyAsync(G, r->G.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(beta, r->beta.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            dW_.ensure(N * N);
+            SQ_CHECK(cudaMemcpyAsync(dW_.p, r->W.data(), 4 * N * N, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(sq103_dense_hamiltonian(dW_.p, (int)N, (int)N, r->optimize, h, J, (int)N, c32, r->c64, scratch,
+                                             st_.get()));
+            SQ_CHECK(sq103_randomize_spins(q, (int)N, m, r->seed, 0, 0, st_.get()));
+            SQ_CHECK(sq103_dense_field_refresh(J, (int)N, q, F, (int)N, m, st_.get()));
+            sq103_dense_task &t = r->dt;
+            t = sq103_dense_task{};
+            t.J = J; t.h = h; t.q = q; t.F = F; t.G = G; t.beta = beta;
+            t.seed = r->seed; t.step0 = 1; t.N = (int)N; t.m = m; t.ldJ = (int)N;
+            t.algo = m == 1 ? kSANaive : kColoring;
+            t.nSteps = n;
+            if (r->large) {
+                ws_.ensure(std::max<unsigned long long>(ws_.n, sq103_dense_ws_bytes((int)N, m, 1)));
+                large_.push_back(r);
+            } else {
+                r->slot = (int)denseSlots_.size();
+                denseSlots_.push_back(r);
+                int zero = 0;
+                SQ_CHECK(cudaMemcpyAsync(dTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
+                SQ_CHECK(cudaMemcpyAsync(dPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+            }
+        } else {
+            const size_t N0 = r->N0, N1 = r->N1;
+            size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh0 = oJ + al(N0 * N1 * 4), oh1 = oh0 + al(N0 * 4),
+                   oc = oh1 + al(N1 * 4), oq0 = oc + 512, oq1 = oq0 + al(m * N0), oF0 = oq1 + al(m * N1),
+                   oF1 = oF0 + al(m * N0 * 4), oR = oF1 + al(m * N1 * 4), tot = oR + al(std::max(m * N1, N0 + N1) * 8);
+            r->mem.ensure(tot);
+            unsigned char *b = r->mem.p;
+            float *G = (float *)(b + oG), *beta = (float *)(b + oB), *J = (float *)(b + oJ);
+            float *h0 = (float *)(b + oh0), *h1 = (float *)(b + oh1), *c32 = (float *)(b + oc);
+            r->c64 = (double *)(b + oc + 256);
+            int8_t *q0 = (int8_t *)(b + oq0), *q1 = (int8_t *)(b + oq1);
+            float *F0 = (float *)(b + oF0), *F1 = (float *)(b + oF1);
+            double *scratch = (double *)(b + oR);
+            SQ_CHECK(cudaMemcpyAsync(G, r->G.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(beta, r->beta.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            dW_.ensure(N0 * N1 + N0 + N1);
+            SQ_CHECK(cudaMemcpyAsync(dW_.p, r->W.data(), 4 * N0 * N1, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(dW_.p + N0 * N1, r->b0.data(), 4 * N0, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(dW_.p + N0 * N1 + N0, r->b1.data(), 4 * N1, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(sq103_bipartite_hamiltonian(dW_.p + N0 * N1, dW_.p + N0 * N1 + N0, dW_.p, (int)N0, (int)N1,
+                                                 r->optimize, h0, h1, J, c32, r->c64, scratch, st_.get()));
+            SQ_CHECK(sq103_randomize_spins(q0, (int)N0, m, r->seed, 0, 0, st_.get()));
+            SQ_CHECK(sq103_randomize_spins(q1, (int)N1, m, r->seed, 0, 1, st_.get()));
+            sq103_bipartite_task &t = r->bt;
+            t = sq103_bipartite_task{};
+            t.J = J; t.h0 = h0; t.h1 = h1; t.q0 = q0; t.q1 = q1; t.F0 = F0; t.F1 = F1;
+            t.G = G; t.beta = beta; t.seed = r->seed; t.step0 = 1;
+            t.N0 = (int)N0; t.N1 = (int)N1; t.m = m;
+            t.algo = m == 1 ? kSAColoring : kColoring;
+            t.nSteps = n;
+            r->slot = (int)bipSlots_.size();
+            bipSlots_.push_back(r);
+            int zero = 0;
+            SQ_CHECK(cudaMemcpyAsync(bTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(bPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+        }
+        st_.sync();  // r->W and the task structs above are read before this returns
+        r->W.clear();
+        r->W.shrink_to_fit();
+    }
+
+    // FP64 energies and spins out, memory and slot released
+    void complete(Request *r) {
+        const int m = r->m;
+        DevBuf<double> E;
+        E.ensure(m);
+        r->E.resize(m);
+        if (r->kind == 0) {
+            const int N = r->N0;
+            double *scratch = (double *)((unsigned char *)r->dt.q + al((size_t)m * N));
+            SQ_CHECK(sq103_dense_energy(r->dt.J, N, r->dt.h, r->c64, r->dt.q, N, m, r->optimize, scratch, E.p, nullptr,
+                                        st_.get()));
+            r->q0.resize((size_t)m * N);
+            SQ_CHECK(cudaMemcpyAsync(r->q0.data(), r->dt.q, (size_t)m * N, cudaMemcpyDeviceToHost, st_.get()));
+        } else {
+            const int N0 = r->N0, N1 = r->N1;
+            double *scratch = (double *)((unsigned char *)r->bt.F1 + al((size_t)m * N1 * 4));
+            SQ_CHECK(sq103_bipartite_energy(r->bt.J, r->bt.h0, r->bt.h1, r->c64, r->bt.q0, r->bt.q1, N0, N1, m,
+                                            r->optimize, scratch, E.p, nullptr, st_.get()));
+            r->q0.resize((size_t)m * N0);
+            r->q1.resize((size_t)m * N1);
+            SQ_CHECK(cudaMemcpyAsync(r->q0.data(), r->bt.q0, (size_t)m * N0, cudaMemcpyDeviceToHost, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(r->q1.data(), r->bt.q1, (size_t)m * N1, cudaMemcpyDeviceToHost, st_.get()));
+        }
+        SQ_CHECK(cudaMemcpyAsync(r->E.data(), E.p, sizeof(double) * m, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        // free the slot: the last slot moves into it
+        if (r->kind == 0 && !r->large) removeSlot(denseSlots_, r, dTasks_.p, dPos_.p, 0);
+        if (r->kind == 1) removeSlot(bipSlots_, r, bTasks_.p, bPos_.p, 1);
+        if (r->large) large_.erase(std::find(large_.begin(), large_.end(), r));
+        st_.sync();
+        r->mem.release();
+        used_ -= r->bytes;
+        active_.erase(r->id);
+        r->state = kDone;
+        ++done_;
+    }
+
+    template <class T>
+    void removeSlot(std::vector<Request *> &slots, Request *r, T *dTasks, int *dPos, int which) {
+        const int s = r->slot, last = (int)slots.size() - 1;
+        if (s != last) {
+            Request *mv = slots[last];
+            SQ_CHECK(cudaMemcpyAsync(dTasks + s, dTasks + last, sizeof(T), cudaMemcpyDeviceToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(dPos + s, dPos + last, sizeof(int), cudaMemcpyDeviceToDevice, st_.get()));
+            slots[s] = mv;
+            mv->slot = s;
+        }
+        slots.pop_back();
+        r->slot = -1;
+        int c = (int)slots.size();
+        hostCount_[which] = c;
+        SQ_CHECK(cudaMemcpyAsync(counts_.p + which, &hostCount_[which], sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+    }
+
+    Stream st_;
+    unsigned long long budget_, used_ = 0;
+    int maxSlots_, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
+    long long ticks_ = 0;
+    int hostCount_[2] = {0, 0};
+    std::map<int, std::unique_ptr<Request>> all_;
+    std::deque<Request *> queue_;
+    std::map<int, Request *> active_;
+    std::vector<Request *> denseSlots_, bipSlots_, large_;
+    DevBuf<sq103_dense_task> dTasks_;
+    DevBuf<sq103_bipartite_task> bTasks_;
+    DevBuf<int> dPos_, bPos_, counts_, queues_;
+    DevBuf<float> dW_;
+    DevBuf<unsigned char> ws_;
+};
+
+}  // namespace sq103
+
+using namespace sq103;
+
+namespace {
+template <class F>
+int serve_guard(F &&f) {
+    try {
+        f();
+        return 0;
+    } catch (const std::exception &e) {
+        sq103_set_error(e.what());
+    } catch (...) {
+        sq103_set_error("unknown error");
+    }
+    return -1;
+}
+Server *as_server(void *h) {
+    throwErrorIf(h == nullptr, "null handle or argument");
+    Server *s = dynamic_cast<Server *>(static_cast<sqaod::NullBase *>(h));
+    throwErrorIf(s == nullptr, "handle of the wrong type");
+    return s;
+}
+}  // namespace
+
+extern "C" {
+
+SQ103_API int sq103_server_new(void **handle, unsigned long long budgetBytes, int maxSlots) {
+    return serve_guard([&] {
+        throwErrorIf(handle == nullptr, "null handle");
+        *handle = static_cast<sqaod::NullBase *>(new Server(budgetBytes, maxSlots > 0 ? maxSlots : 4096));
+    });
+}
+SQ103_API int sq103_server_delete(void *h) { return serve_guard([&] { delete as_server(h); }); }
+SQ103_API int sq103_server_submit_dense(void *h, const float *W, int N, int m, int optimize, unsigned long long seed,
+                                        const float *G, const float *beta, int nSteps, int *id) {
+    return serve_guard([&] {
+        throwErrorIf(!W || !G || !beta, "null argument");
+        int i = as_server(h)->submitDense(W, N, m, optimize, seed, G, beta, nSteps);
+        if (id) *id = i;
+    });
+}
+SQ103_API int sq103_server_submit_bipartite(void *h, const float *b0, const float *b1, const float *W, int N0, int N1,
+                                            int m, int optimize, unsigned long long seed, const float *G,
+                                            const float *beta, int nSteps, int *id) {
+    return serve_guard([&] {
+        throwErrorIf(!b0 || !b1 || !W || !G || !beta, "null argument");
+        int i = as_server(h)->submitBipartite(b0, b1, W, N0, N1, m, optimize, seed, G, beta, nSteps);
+        if (id) *id = i;
+    });
+}
+SQ103_API int sq103_server_tick(void *h, int *completed) {
+    return serve_guard([&] {
+        int c = as_server(h)->tick();
+        if (completed) *completed = c;
+    });
+}
+SQ103_API int sq103_server_state(void *h, int id, int *state) {
+    return serve_guard([&] { *state = as_server(h)->state(id); });
+}
+SQ103_API int sq103_server_result(void *h, int id, double *E, int capE, int *m, int8_t *q0, int8_t *q1,
+                                  long long capBytes, int release) {
+    return serve_guard([&] {
+        Server *s = as_server(h);
+        const Server::Request &r = s->request(id);
+        throwErrorIf(r.state != Server::kDone, "request %d is not done.", id);
+        throwErrorIf((int)r.E.size() > capE, "energy capacity %d is smaller than %d.", capE, (int)r.E.size());
+        if (E) memcpy(E, r.E.data(), sizeof(double) * r.E.size());
+        if (m) *m = r.m;
+        throwErrorIf((long long)r.q0.size() > capBytes || (long long)r.q1.size() > capBytes, "spin capacity too small.");
+        if (q0) memcpy(q0, r.q0.data(), r.q0.size());
+        if (q1 && !r.q1.empty()) memcpy(q1, r.q1.data(), r.q1.size());
+        if (release) s->release(id);
+    });
+}
+SQ103_API int sq103_server_stats(void *h, int *queued, int *active, int *done, unsigned long long *bytesInUse) {
+    return serve_guard([&] { as_server(h)->stats(queued, active, done, bytesInUse); });
+}
+
+}  // extern "C"
