@@ -124,6 +124,10 @@ SQ103_API int sq103_dense_batch_launch(const sq103_dense_task *d_tasks, int nTas
                                        const int *d_order, int *d_pos, int *d_queue, int stepsPerLaunch, int grid,
                                        int smemBytes, void *stream);
 SQ103_API int sq103_dense_batch_max_smem(void);
+/* Least smemBytes a batch launch needs when its largest instance has maxM
+ * trotters (the per-phase flip lists); an instance whose lists do not fit is
+ * skipped, its pos unchanged and 3 (capacity) written to its status. */
+SQ103_API int sq103_dense_batch_min_smem(int maxM);
 SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes);
 
 /* -------------------------------------------- kernel layer: bipartite */
@@ -322,8 +326,9 @@ SQ103_API int sq103_dense_batch_get_q(void *handle, int index, int8_t *q, int ca
  * sq103_server_tick advances every active instance by one annealOneStep and
  * completes the finished ones (FP64 energies, spins).  Each request ends
  * exactly as the same seed and schedule would alone (sq103_dg_annealer /
- * sq103_bg_annealer with prepare, randomize_spin and the schedule).
- * States: 0 queued, 1 active, 2 done. */
+ * sq103_bg_annealer with prepare, randomize_spin and the schedule; the
+ * coloring algorithm for m > 1, sa_naive (dense) or sa_coloring (bipartite)
+ * for m == 1).  States: 0 queued, 1 active, 2 done. */
 SQ103_API int sq103_server_new(void **handle, unsigned long long budgetBytes, int maxSlots);
 SQ103_API int sq103_server_delete(void *handle);
 SQ103_API int sq103_server_submit_dense(void *handle, const float *W, int N, int m, int optimize,

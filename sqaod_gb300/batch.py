@@ -3,7 +3,7 @@
 Every annealOneStep of all instances is one persistent kernel launch,
 replayed from a CUDA graph, with instances taken from a queue largest first.
 Each instance follows exactly the rules of the single-instance annealer
-(coloring sweep, Philox stream of its seed, field refresh every 8 steps), so
+(coloring sweep, sa_naive for one trotter, Philox stream of its seed, field refresh every 8 steps), so
 an instance annealed in a batch ends in the same state as when annealed alone
 with sqaod_gb300.cuda.dense_graph_annealer and the same seed.
 """

@@ -57,14 +57,25 @@ __device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F,
     }
 }
 
+// Dynamic shared memory every launch of anneal_instance needs: the flip lists
+// of two phases (2 m entries) and their counters, rounded to 16 bytes.
+__host__ __device__ constexpr size_t flip_list_bytes(int m) {
+    return ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
+}
+
 // One CTA anneals one instance (all trotters) for steps [s0, s0 + nSteps) of
 // its schedule.  Spins, fields and h are staged in shared memory when they
-// fit; otherwise the CTA works on global memory.
-__device__ void anneal_instance(const sq103_dense_task &T, unsigned char *smem, int smemBytes, int s0, int nSteps) {
+// fit; otherwise the CTA works on global memory.  Returns false, without
+// touching the instance, when smemBytes cannot hold the flip lists.
+__device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, int smemBytes, int s0, int nSteps) {
     const int N = T.N, m = T.m, tid = threadIdx.x;
+    const size_t off = flip_list_bytes(m);
+    if (off > (size_t)smemBytes) {
+        if (tid == 0 && T.status) atomicExch(T.status, kErrCapacity);
+        return false;
+    }
     Flip *flips = reinterpret_cast<Flip *>(smem);            // 2 x m
     int *nflip = reinterpret_cast<int *>(flips + 2 * m);      // 2 counters
-    size_t off = ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
     size_t stageBytes = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
     const bool stage = off + stageBytes <= (size_t)smemBytes;
     float *F;
@@ -191,6 +202,7 @@ __device__ void anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
         }
     }
     __syncthreads();  // shared memory is reused by the CTA's next instance
+    return true;
 }
 
 __global__ void __launch_bounds__(kBlockThreads) dense_sweep_cta(const sq103_dense_task *tasks,
@@ -221,10 +233,7 @@ __global__ void __launch_bounds__(kBlockThreads) dense_batch_persistent(const sq
         const sq103_dense_task T = tasks[ti];
         const int s0 = pos[ti];
         const int n = min(stepsPerLaunch, T.nSteps - s0);
-        if (n > 0) {
-            anneal_instance(T, smem, smemBytes, s0, n);
-            if (threadIdx.x == 0) pos[ti] = s0 + n;
-        }
+        if (n > 0 && anneal_instance(T, smem, smemBytes, s0, n) && threadIdx.x == 0) pos[ti] = s0 + n;
     }
     // the last CTA to leave resets the queue for the next replay
     if (threadIdx.x == 0) {
@@ -270,7 +279,7 @@ static int max_dyn_smem() {
 }
 
 static size_t cta_smem_bytes(int N, int m) {
-    size_t base = ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
+    size_t base = flip_list_bytes(m);
     size_t stage = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
     size_t lim = (size_t)max_dyn_smem();
     if (base + stage <= lim) return base + stage;
@@ -334,6 +343,8 @@ static int batch_dyn_smem() {
 }
 
 SQ103_API int sq103_dense_batch_max_smem(void) { return batch_dyn_smem(); }
+
+SQ103_API int sq103_dense_batch_min_smem(int maxM) { return maxM > 0 ? (int)flip_list_bytes(maxM) : 0; }
 
 SQ103_API int sq103_dense_batch_ctas_per_sm(int smemBytes) {
     int perSm = 0;

@@ -60,6 +60,8 @@ public:
         bPos_.ensure(maxSlots);
         counts_.ensure(2);
         queues_.ensure(4);
+        status_.ensure(1);
+        SQ_CHECK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_.get()));
         SQ_CHECK(cudaMemsetAsync(queues_.p, 0, sizeof(int) * 4, st_.get()));
         SQ_CHECK(cudaMemsetAsync(counts_.p, 0, sizeof(int) * 2, st_.get()));
         int dev = 0;
@@ -74,6 +76,8 @@ public:
     int submitDense(const float *W, int N, int m, int optimize, unsigned long long seed, const float *G,
                     const float *beta, int nSteps) {
         throwErrorIf(N <= 0 || m <= 0 || nSteps <= 0, "bad request shape.");
+        throwErrorIf(sq103_dense_batch_min_smem(m) > stageSmem_ && !sq103_dense_multicta_ok(N, m, kColoring),
+                     "%d trotters of %d spins fit neither kernel.", m, N);
         for (int r = 0; r < N; ++r)
             for (int c = 0; c < r; ++c)
                 throwErrorIf(W[(size_t)r * N + c] != W[(size_t)c * N + r], "%s, Matrix is not symmetric.", __func__);
@@ -246,6 +250,7 @@ private:
             t.seed = r->seed; t.step0 = 1; t.N = (int)N; t.m = m; t.ldJ = (int)N;
             t.algo = m == 1 ? kSANaive : kColoring;
             t.nSteps = n;
+            t.status = status_.p;
             if (r->large) {
                 ws_.ensure(std::max<unsigned long long>(ws_.n, sq103_dense_ws_bytes((int)N, m, 1)));
                 large_.push_back(r);
@@ -321,7 +326,10 @@ private:
             SQ_CHECK(cudaMemcpyAsync(r->q1.data(), r->bt.q1, (size_t)m * N1, cudaMemcpyDeviceToHost, st_.get()));
         }
         SQ_CHECK(cudaMemcpyAsync(r->E.data(), E.p, sizeof(double) * m, cudaMemcpyDeviceToHost, st_.get()));
+        int status = 0;
+        SQ_CHECK(cudaMemcpyAsync(&status, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
+        throwErrorIf(status != 0, "a dense sweep kernel reported status %d.", status);
         // free the slot: the last slot moves into it
         if (r->kind == 0 && !r->large) removeSlot(denseSlots_, r, dTasks_.p, dPos_.p, 0);
         if (r->kind == 1) removeSlot(bipSlots_, r, bTasks_.p, bPos_.p, 1);
@@ -362,7 +370,7 @@ private:
     std::vector<Request *> denseSlots_, bipSlots_, large_;
     DevBuf<sq103_dense_task> dTasks_;
     DevBuf<sq103_bipartite_task> bTasks_;
-    DevBuf<int> dPos_, bPos_, counts_, queues_;
+    DevBuf<int> dPos_, bPos_, counts_, queues_, status_;
     DevBuf<float> dW_;
     DevBuf<unsigned char> ws_;
 };

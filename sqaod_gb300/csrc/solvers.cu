@@ -1224,8 +1224,12 @@ public:
         int dev = 0, sms = 0;
         SQ_CHECK(cudaGetDevice(&dev));
         SQ_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        int maxS = sq103_dense_batch_max_smem();
+        int maxS = sq103_dense_batch_max_smem(), maxM = 1;
+        for (auto &p : insts_) maxM = std::max(maxM, p->m);
+        const int minS = sq103_dense_batch_min_smem(maxM);  // the flip lists of the largest m
+        throwErrorIf(minS > maxS, "%d trotters exceed the shared memory of one CTA.", maxM);
         smem_ = smemBytes < 0 ? std::min(maxS, 96 * 1024) : std::min(smemBytes, maxS);
+        smem_ = std::max(smem_, minS);
         int per = std::max(1, sq103_dense_batch_ctas_per_sm(smem_));
         grid_ = std::max(1, std::min((int)insts_.size(), per * sms));
         if (graph_) {

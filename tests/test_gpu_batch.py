@@ -42,7 +42,8 @@ def test_batch_equals_single(use_graph):
     b.anneal(len(G), use_graph=use_graph)
     assert b.info()["position"] == len(G)
     for i, (W, m, seed) in enumerate(probs):
-        a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm="coloring")
+        # one trotter runs simulated annealing in the batch
+        a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm="sa_naive" if m == 1 else "coloring")
         a.set_kernel(1)
         a.seed(seed)
         a.prepare()
