@@ -100,6 +100,24 @@ SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q
 SQ103_API int sq103_dense_energy(const float *J, int ldJ, const float *h, const double *c64,
                                  const int8_t *q, int N, int m, int maximize, double *r_scratch,
                                  double *E64, float *E32, void *stream);
+/* sq103_dense_energy without a caller-supplied scratch buffer; it has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory: code inside a framework whose pool owns all device memory,
+ * or a service that must not grow its footprint after start-up.  The m x N
+ * FP64 row sums live in a static device array of
+ * sq103_dense_energy_static_max() = 262144 doubles (2 MiB, held by every GPU
+ * that loads the library); m * N above that returns 3 (capacity) with a
+ * message in sq103_last_error() and launches nothing.  Nothing is allocated
+ * and nothing needs to start at zero (every scratch value is written before
+ * it is read).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current); make that first
+ * call before any stream capture.  One scratch array serves all callers of a
+ * device: calls that overlap in time (other streams, other threads) race on
+ * it and must be serialised by the caller. */
+SQ103_API unsigned long long sq103_dense_energy_static_max(void);
+SQ103_API int sq103_dense_energy_static(const float *J, int ldJ, const float *h, const double *c64,
+                                        const int8_t *q, int N, int m, int maximize, double *E64, float *E32,
+                                        void *stream);
 /* sum_y q_y . q_{y+1} (DeviceDotSpins, sqaodc/cuda/DeviceBatchedDot.cuh:145-160) */
 SQ103_API int sq103_ring_dot(const int8_t *q, int N, int m, long long *out, void *stream);
 /* randomizeSpin (sqaodc/cuda/DeviceKernels.cu:550-572) from the Philox stream */

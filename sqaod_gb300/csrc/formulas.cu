@@ -240,6 +240,73 @@ SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const floa
     return (int)cudaGetLastError();
 }
 
+}  // extern "C"
+
+// ------------------------------------------------ no-allocation energy entry point
+// sq103_dense_energy_static serves callers that cannot allocate device memory:
+// code running inside a framework whose memory pool owns the whole device (a
+// cudaMalloc there fails or fragments the pool), or a long-lived service that
+// must keep its footprint fixed after start-up.  Its scratch, one m x N block
+// of FP64 row sums, is this file-scope device array: every GPU that loads the
+// library holds its kStaticEnergyElems doubles (2 MiB) until the process
+// exits.  The spin GEMM writes every value it later reads, so nothing has to
+// be cleared between calls.  There is one array per device: two calls that
+// overlap in time (different streams or threads) race on it, so callers must
+// serialise them.
+static constexpr size_t kStaticEnergyElems = (size_t)1 << 18;
+static __device__ __align__(256) double g_energy_scratch[kStaticEnergyElems];
+
+namespace {
+// device address of g_energy_scratch, looked up with cudaGetSymbolAddress by
+// the first call on each device, with that device current (the host-side
+// name is only a stand-in for the symbol).  That lookup is the call's only
+// set-up work; make the first call on a device before any stream capture.
+std::mutex g_scratch_mutex;
+double *g_scratch_addr[256] = {};
+
+int static_scratch(double **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= 256) return kErrBadShape;
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_energy_scratch);
+        if (e != cudaSuccess) return (int)e;
+        g_scratch_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+SQ103_API unsigned long long sq103_dense_energy_static_max(void) { return (unsigned long long)kStaticEnergyElems; }
+
+SQ103_API int sq103_dense_energy_static(const float *J, int ldJ, const float *h, const double *c64, const int8_t *q,
+                                        int N, int m, int maximize, double *E64, float *E32, void *stream) {
+    if (N <= 0 || m <= 0) {
+        sq103_set_error("sq103_dense_energy_static: N and m must be positive.");
+        return kErrBadShape;
+    }
+    if ((size_t)N * (size_t)m > kStaticEnergyElems) {
+        char msg[160];
+        snprintf(msg, sizeof(msg), "sq103_dense_energy_static: m * N = %zu exceeds the static scratch of %zu values.",
+                 (size_t)N * (size_t)m, kStaticEnergyElems);
+        sq103_set_error(msg);
+        return kErrCapacity;
+    }
+    double *scratch = nullptr;
+    int rc = static_scratch(&scratch);
+    if (rc != 0) {
+        sq103_set_error("sq103_dense_energy_static: cudaGetSymbolAddress of the static scratch failed.");
+        return rc;
+    }
+    return sq103_dense_energy(J, ldJ, h, c64, q, N, m, maximize, scratch, E64, E32, stream);
+}
+
 SQ103_API int sq103_ring_dot(const int8_t *q, int N, int m, long long *out, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaMemsetAsync(out, 0, sizeof(long long), s);
