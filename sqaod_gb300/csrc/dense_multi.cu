@@ -6,25 +6,44 @@
 // bit-identical spins and fields.
 //
 // Per CTA (trotter y), 256 threads:
-//   warp 0  decider: trials in batches of 32 iterations, lane i = iteration g0+i.
-//           Lane i starts from its site's resident field F[y][x_i] (exact
-//           through the previous batch) and, as earlier lanes accept, adds
-//           d_j * J[x_j][x_i] in trial order (the gathers J[x_j][x_i] are
-//           loaded one batch ahead).  The batch's accept bits go to a global
-//           accept log, followed by a release store of the progress word.
-//   warp 1  helper: for each ring neighbour n (trotters y-1, y+1 in other
-//           CTAs) it replays n's Philox site stream into a ring of sites, and
-//           applies n's published accept log to a ghost bit row of n's spins.
-//   warps 2-7 updaters: after each batch, F[y][:] += d * J[x][:] for the batch's
-//           accepted flips, in trial order (float4 rows of J from L2/HBM).
+//   warp 0  decider: the trotter's trials in batches of 32 iterations, lane i =
+//           iteration g0 + i.  A batch is decided in rounds: every undecided
+//           lane evaluates its trial with its current field and neighbour
+//           spins; the lowest accepting lane is final (all undecided lanes
+//           below it reject), and the lanes above it add d * J[x_f][x_i] to
+//           their fields and flip their spin copy when they share its site.
+//           A batch takes (accepted flips + 1) rounds instead of 32 sequential
+//           trials.  The batch's fields start from the resident row F[y][:],
+//           which the updaters keep one batch behind, plus the previous
+//           batch's flips d_f * J[x_f][x_i], gathered at the batch boundary and
+//           added after the neighbour work of the next batch.
+//           Decisions are published as one 64-bit word per batch (accept
+//           bits, decided count, batch tag) with a single relaxed store after
+//           every accepting round and at the end of the batch: a reader that
+//           sees the tag of the batch it wants sees consistent bits, so no
+//           fence is needed.
+//   warp 1  helper: polls the two neighbours' accept words (both neighbours,
+//           two words ahead, in one round trip) and copies them into shared
+//           memory.
+//   warps 2-3 prefetchers, alternate batches: this trotter's own sites,
+//           uniforms and step constants, the in-batch gathers J[x_j][x_i]
+//           (j < i), and the neighbours' sites of the same iterations (a ring
+//           of sites, a count table hashed site -> neighbour trials not yet
+//           applied, and a last-trial table hashed site -> latest such trial),
+//           into a ring of kPre batch buffers with a ready tag each.
+//   warps 4-7 updaters: F[y][:] += d * J[x][:] for the flips of the previous
+//           batch, in trial order, while the decider works on the next one.
 // Colour order: trial (y, k) must see neighbour n after every neighbour trial
 // that precedes it (iteration < k, or = k when n's colour phase comes first:
-// even trotters, then trotter m-1 if m is odd, then odd trotters).  Only
-// neighbour trials at the same site matter, so a trial waits only when a
-// neighbour trial inside the not-yet-applied window hit its site; the wait is
-// bounded (global timer) and ends the kernel with a timeout status instead of
-// hanging.  Before waiting a CTA publishes its own progress, so waits always
-// point to strictly earlier trials and cannot form a cycle.
+// even trotters, then trotter m-1 if m is odd, then odd trotters).  The
+// decider applies neighbour flips to a ghost bit row of n only up to the
+// first trial of its current batch; each lane corrects its site for the
+// neighbour trials between that point and its own limit, which the count
+// table shows to be none for almost every lane.  A lane waits only when such
+// a neighbour trial is not yet published.  Every wait is bounded (global
+// timer) and ends the kernel with a timeout status instead of hanging; before
+// waiting a CTA publishes the trials it has decided, so waits always point to
+// strictly earlier trials and cannot form a cycle.
 #include <cooperative_groups.h>
 
 #include "sq_common.cuh"
@@ -33,26 +52,61 @@
 namespace sq103 {
 
 constexpr int kMcThreads = 256;
-constexpr int kMcUpdaters = kMcThreads - 64;
-constexpr int kRing = 256;  // iterations of neighbour sites kept (power of two)
+constexpr int kPf = 2;                            // prefetcher warps (2 .. 1 + kPf)
+constexpr int kUpdWarp0 = 2 + kPf;                // first updater warp
+constexpr int kMcUpdaters = kMcThreads - 32 * kUpdWarp0;
+constexpr int kBarCount = 32 + kMcUpdaters;       // decider + updaters
+constexpr int kRing = 256;      // neighbour sites kept per neighbour (power of two)
+constexpr int kLogWords = 32;   // neighbour accept words kept per neighbour (power of two)
+constexpr int kHash = 2048;     // count / last-trial table entries per neighbour (power of two)
+constexpr int kPre = 4;         // prefetched batches (power of two)
+constexpr int kJgStride = 32 * 33;
+constexpr int kGv = 16;         // flips of a batch whose gathers are deferred to the next batch
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;
-constexpr int kProgStride = 32;  // progress words on their own 128-byte lines
+constexpr unsigned FULL = 0xffffffffu;
 
-__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_gpu(unsigned *p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-__device__ __forceinline__ void named_bar(int id, int n) {
+__device__ __forceinline__ void bar_sync(int id, int n) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ unsigned smem_addr(const volatile void *p) {
+    return (unsigned)__cvta_generic_to_shared((const void *)p);
+}
+__device__ __forceinline__ int ld_acquire_cta(const volatile int *p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_acquire_cta64(const volatile unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.cta.shared.b64 %0, [%1];" : "=l"(v) : "r"(smem_addr(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cta(volatile int *p, int v) {
+    asm volatile("st.release.cta.shared.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_cta64(volatile unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.cta.shared.b64 [%0], %1;" ::"r"(smem_addr(p)), "l"(v) : "memory");
+}
+
+// accept word of batch b: bits 0-31 accept bits, 32-37 decided count, 38-63 b + 1
+__device__ __forceinline__ unsigned long long log_word(int b, int cnt, unsigned bits) {
+    return ((unsigned long long)(b + 1) << 38) | ((unsigned long long)cnt << 32) | bits;
 }
 
 __host__ __device__ __forceinline__ int colour_phase(int y, int m) {
@@ -61,33 +115,101 @@ __host__ __device__ __forceinline__ int colour_phase(int y, int m) {
 }
 
 struct McShared {
-    volatile int applied[2];   // neighbour iterations applied to the ghost rows
-    volatile int ringHead[2];  // neighbour sites computed for iterations < ringHead
+    volatile unsigned long long logAvail;  // neighbour accept bits known below (lo: neighbour 0, hi: 1) (helper)
+    volatile int applied[2];               // neighbour iterations applied to the ghost rows (decider)
+    volatile int readyTag[kPre];           // p + 1 once buffer p % kPre holds batch p (prefetchers)
+    volatile int decDone;                  // batches [0, decDone) no longer read from the buffers (decider)
     volatile int done;
-    volatile int nflip;
+    int nflip;
 };
 
-__global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task T, uint32_t *outLog,
-                                                                unsigned *progress, int nWords) {
+// every lane loads the flag with acquire semantics (one broadcast access); the
+// value of lane 0 keeps control flow uniform
+__device__ __forceinline__ int uniform_acquire(const volatile int *p) { return __shfl_sync(FULL, ld_acquire_cta(p), 0); }
+__device__ __forceinline__ unsigned long long uniform_acquire64(const volatile unsigned long long *p) {
+    return __shfl_sync(FULL, ld_acquire_cta64(p), 0);
+}
+__device__ __forceinline__ int avail_of(unsigned long long v, int n) { return (int)(n ? v >> 32 : v & 0xffffffffu); }
+
+// bounded wait on a warp-uniform condition; false on timeout
+template <class F>
+__device__ __forceinline__ bool wait_until(F &&ready) {
+    unsigned long long t0 = 0;
+    while (!ready()) {
+        if (t0 == 0) t0 = global_ns();
+        if (global_ns() - t0 > kWaitLimitNs) return false;
+        __nanosleep(32);
+    }
+    return true;
+}
+
+// Neighbour spin bit at site x as of neighbour iteration Ji, from the ghost row
+// (iterations < A applied) and the published accept bits of iterations [A, Ji]
+// that hit x.  cnt[h] counts the neighbour iterations since A whose site hashes
+// to h and lastJ[h] is the latest of them; the prefetchers raise cnt before
+// lastJ, and lastJ is read first here, so a count of one with lastJ outside
+// [A, Ji] means the only such iteration comes after Ji.  Returns false (need =
+// latest unpublished iteration at x) when the bit cannot be known yet.
+__device__ __forceinline__ bool nbr_bit(int x, int Ji, int A, int avail, const uint32_t *ghost,
+                                        const volatile int *lastJ, const volatile int *cnt,
+                                        const volatile int *ring, const volatile uint32_t *nlog, int &bit,
+                                        int &need) {
+    bit = (ghost[x >> 5] >> (x & 31)) & 1;
+    need = -1;
+    const int h = x & (kHash - 1);
+    const int jl = lastJ[h];
+    const int c = cnt[h];
+    if (c == 0) return true;
+    if (c == 1) {
+        if (jl < A || jl > Ji || ring[jl & (kRing - 1)] != x) return true;
+        if (jl < avail) {
+            bit ^= (nlog[(jl >> 5) & (kLogWords - 1)] >> (jl & 31)) & 1;
+            return true;
+        }
+        need = jl;
+        return false;
+    }
+    for (int j = A; j <= Ji; ++j) {
+        if (ring[j & (kRing - 1)] != x) continue;
+        if (j < avail)
+            bit ^= (nlog[(j >> 5) & (kLogWords - 1)] >> (j & 31)) & 1;
+        else
+            need = j;
+    }
+    return need < 0;
+}
+
+__global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_task T, unsigned long long *outLog,
+                                                                   int nWords) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ McShared S;
-    const unsigned FULL = 0xffffffffu;
     const int y = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = T.N, m = T.m;
     const bool sa = T.algo == kSANaive;
     const int nNbr = sa ? 0 : (m == 2 ? 1 : 2);
     const int nbr0 = (y + m - 1) % m, nbr1 = (y + 1) % m;
+    const int myPh = colour_phase(y, m);
+    const int before0 = colour_phase(nbr0, m) < myPh ? 1 : 0;
+    const int before1 = colour_phase(nbr1, m) < myPh ? 1 : 0;
     const int Itot = T.nSteps * N;
+    const int nBatches = (Itot + 31) / 32;
     const int nWG = (N + 31) / 32;
+    const int ghostStride = (nWG + 1) & ~1;
     const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
 
-    float *Fs = reinterpret_cast<float *>(smem);                 // N
-    float *hs = Fs + N;                                          // N
-    float *Jgs = hs + N;                                         // 32 x 33 gathers
-    uint32_t *ghost = reinterpret_cast<uint32_t *>(Jgs + 32 * 33);  // 2 x nWG
-    int *ring = reinterpret_cast<int *>(ghost + 2 * nWG);         // 2 x kRing
-    int2 *flips = reinterpret_cast<int2 *>(ring + 2 * kRing);     // 32
-    int8_t *qs = reinterpret_cast<int8_t *>(flips + 32);          // N
+    float *Fs = reinterpret_cast<float *>(smem);                        // N
+    float *hs = Fs + N;                                                 // N
+    float *Jg = hs + N;                                                 // kPre x 32 x 33
+    float *preU = Jg + kPre * kJgStride;                                // kPre x 32
+    float *preC = preU + kPre * 32;                                     // kPre x 3 x 32
+    int *preX = reinterpret_cast<int *>(preC + kPre * 96);              // kPre x 32
+    uint32_t *ghost = reinterpret_cast<uint32_t *>(preX + kPre * 32);   // 2 x ghostStride
+    int *lastJ = reinterpret_cast<int *>(ghost + 2 * ghostStride);      // 2 x kHash
+    int *cnt = lastJ + 2 * kHash;                                       // 2 x kHash
+    int *ring = cnt + 2 * kHash;                                        // 2 x kRing
+    uint32_t *nlog = reinterpret_cast<uint32_t *>(ring + 2 * kRing);    // 2 x kLogWords
+    int2 *flips = reinterpret_cast<int2 *>(nlog + 2 * kLogWords);       // 32
+    int8_t *qs = reinterpret_cast<int8_t *>(flips + 32);                // N
 
     for (int i = tid; i < N; i += kMcThreads) {
         Fs[i] = T.F[(size_t)y * N + i];
@@ -99,12 +221,18 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
         for (int w = tid; w < nWG; w += kMcThreads) {
             uint32_t bits = 0;
             for (int b = 0; b < 32 && w * 32 + b < N; ++b) bits |= (qn[w * 32 + b] > 0 ? 1u : 0u) << b;
-            ghost[n * nWG + w] = bits;
+            ghost[n * ghostStride + w] = bits;
         }
     }
+    for (int i = tid; i < 2 * kHash; i += kMcThreads) {
+        lastJ[i] = -1;
+        cnt[i] = 0;
+    }
     if (tid == 0) {
+        S.logAvail = 0;
         S.applied[0] = S.applied[1] = 0;
-        S.ringHead[0] = S.ringHead[1] = 0;
+        for (int i = 0; i < kPre; ++i) S.readyTag[i] = 0;
+        S.decDone = 0;
         S.done = 0;
         S.nflip = 0;
     }
@@ -114,150 +242,209 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
 
     if (warp == 0) {
         // ------------------------------------------------------------ decider
-        const int myPh = colour_phase(y, m);
-        const int before0 = colour_phase(nbr0, m) < myPh ? 1 : 0;
-        const int before1 = colour_phase(nbr1, m) < myPh ? 1 : 0;
         const uint32_t wordsPerStep = (uint32_t)(((size_t)N * m + 31) / 32);
         unsigned long long accepted = 0;
         bool aborted = false;
+        int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
+        int nfPrev = 0;      // flips of the previous batch still to be added to Fv
+        float gv[kGv];       // their gathers J[x_f][x] (at this batch's sites)
+#pragma unroll
+        for (int t = 0; t < kGv; ++t) gv[t] = 0.f;
 
-        // per-lane trial state of the current batch and the next one
-        auto trial_setup = [&](int g, int &x, float &u, StepConst &sc, int &s, int &k) {
-            s = g / N;
-            k = g - s * N;
-            u32x4 r = draw(T.seed, (uint32_t)k, (uint32_t)y, T.step0 + (uint32_t)s, tag);
-            x = draw_index(r.x, N);
-            u = draw_unit(r.y);
-            float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
-            sc = step_const(T.algo, m, G, beta);
+        // Applies the published neighbour trials below lim0 / lim1 (their sites are in
+        // the ring) to the ghost rows; returns the helper's availability word.
+        auto apply_nbr = [&](int lim0, int lim1) {
+            const unsigned long long av = uniform_acquire64(&S.logAvail);
+            lim0 = min(avail_of(av, 0), lim0);
+            lim1 = nNbr > 1 ? min(avail_of(av, 1), lim1) : 0;
+            const int span = max(lim0 - A0, lim1 - A1);
+            for (int j0 = 0; j0 < span; j0 += 32) {
+#pragma unroll
+                for (int n = 0; n < 2; ++n) {
+                    const int j = (n ? A1 : A0) + j0 + lane;
+                    if (n < nNbr && j < (n ? lim1 : lim0)) {
+                        const int site = ring[n * kRing + (j & (kRing - 1))];
+                        atomicSub(&cnt[n * kHash + (site & (kHash - 1))], 1);
+                        if ((nlog[n * kLogWords + ((j >> 5) & (kLogWords - 1))] >> (j & 31)) & 1u)
+                            atomicXor(&ghost[n * ghostStride + (site >> 5)], 1u << (site & 31));
+                    }
+                }
+            }
+            if (span > 0) {
+                A0 = max(A0, lim0);
+                if (nNbr > 1) A1 = max(A1, lim1);
+                __syncwarp();
+                if (lane == 0) {
+                    S.applied[0] = A0;
+                    S.applied[1] = A1;
+                }
+            }
+            return av;
         };
 
-        int x = 0, s = 0, k = 0;
-        float u = 0.f;
-        StepConst sc = {0.f, 0.f, 0.f};
-        {
-            int g = lane;
-            if (g < Itot) trial_setup(g, x, u, sc, s, k);
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                int xi = __shfl_sync(FULL, x, i);
-                Jgs[lane * 33 + i] = (i < lane && g < Itot) ? __ldg(T.J + (size_t)xi * T.ldJ + x) : 0.f;
-            }
-            __syncwarp();
-        }
+        aborted = !wait_until([&] { return uniform_acquire(&S.readyTag[0]) == 1; });
+        int x = preX[lane];
+        float Fv = Fs[x];
 
-        for (int g0 = 0; g0 < Itot && !aborted; g0 += 32) {
+        for (int b = 0; b < nBatches && !aborted; ++b) {
+            const int g0 = b * 32;
+            const int buf = b & (kPre - 1);
             const int nValid = min(32, Itot - g0);
             const bool valid = lane < nValid;
-            float Fv = valid ? Fs[x] : 0.f;
+            const float u = preU[buf * 32 + lane];
+            const StepConst sc = {preC[buf * 96 + lane], preC[buf * 96 + 32 + lane], preC[buf * 96 + 64 + lane]};
+            const float *jg = Jg + buf * kJgStride + lane * 33;
             const float hx = valid ? hs[x] : 0.f;
+            float qx = valid ? (float)qs[x] : 1.f;
 
-            // next batch: sites and gathers in flight while this batch is decided
-            int xN = 0, sN = 0, kN = 0;
-            float uN = 0.f;
-            StepConst scN = {0.f, 0.f, 0.f};
-            const int gN = g0 + 32 + lane;
-            const bool validN = gN < Itot;
-            if (validN) trial_setup(gN, xN, uN, scN, sN, kN);
-            float Jn[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                int xi = __shfl_sync(FULL, xN, i);
-                Jn[i] = (i < lane && validN) ? __ldg(T.J + (size_t)xi * T.ldJ + xN) : 0.f;
+            // neighbour spins at this batch's sites: apply the published neighbour
+            // trials before this batch's first trial (both neighbours in one pass;
+            // their sites are in the ring since this batch's buffer is ready)
+            int qb0 = 0, qb1 = 0, nd0 = -1, nd1 = -1;
+            unsigned blocked = 0;
+            if (nNbr > 0) {
+                const unsigned long long av = apply_nbr(g0 + before0, g0 + before1);
+                if (valid) {
+                    bool known = nbr_bit(x, g0 + lane - 1 + before0, A0, avail_of(av, 0), ghost, lastJ, cnt, ring,
+                                         nlog, qb0, nd0);
+                    if (nNbr > 1)
+                        known &= nbr_bit(x, g0 + lane - 1 + before1, A1, avail_of(av, 1), ghost + ghostStride,
+                                         lastJ + kHash, cnt + kHash, ring + kRing, nlog + kLogWords, qb1, nd1);
+                    if (!known) blocked = 1u << lane;
+                }
+                blocked = __reduce_or_sync(FULL, blocked);
             }
 
-            unsigned accBits = 0;
-            int nf = 0;
-            int published = g0;  // iterations [0, published) are visible to the neighbours
-            for (int i = 0; i < nValid; ++i) {
-                const int xi = __shfl_sync(FULL, x, i);
-                const int gi = g0 + i;
-                float qn[2] = {0.f, 0.f};
-                for (int n = 0; n < nNbr; ++n) {
-                    const int Jlim = gi - 1 + (n ? before1 : before0);
-                    unsigned long long tStart = 0;
-                    int bit = 0;
-                    for (;;) {
-                        int a = __shfl_sync(FULL, S.applied[n], 0);
-                        int head = __shfl_sync(FULL, S.ringHead[n], 0);
-                        bool ready = false;
-                        if (Jlim < a) {
-                            ready = true;
-                        } else if (Jlim < head && Jlim - a < kRing) {
-                            int jc = -1;
-                            for (int j0 = a; j0 <= Jlim; j0 += 32) {
-                                int j = j0 + lane;
-                                bool hit = j <= Jlim && ring[n * kRing + (j & (kRing - 1))] == xi;
-                                unsigned b = __ballot_sync(FULL, hit);
-                                if (b) jc = j0 + 31 - __clz(b);
-                            }
-                            ready = jc < 0;
-                        }
-                        if (ready) break;
-                        if (published < gi) {  // publish everything decided before waiting
-                            if (lane == 0) {
-                                __stcg(outLog + (size_t)y * nWords + (g0 >> 5), accBits);
-                                st_release_gpu(progress + (size_t)y * kProgStride, (unsigned)gi);
-                            }
-                            published = gi;
-                        }
-                        if (tStart == 0) tStart = global_ns();
-                        if (global_ns() - tStart > kWaitLimitNs) {
-                            aborted = true;
-                            break;
-                        }
-                        __nanosleep(64);
-                    }
-                    if (aborted) break;
-                    __threadfence_block();
-                    bit = (ghost[n * nWG + (xi >> 5)] >> (xi & 31)) & 1u;
-                    qn[n] = bit ? 1.f : -1.f;
-                }
-                if (aborted) break;
-                if (nNbr == 1) qn[1] = qn[0];
+            // the previous batch's flips (gathered at the end of that batch)
+#pragma unroll
+            for (int t = 0; t < kGv; ++t)
+                if (t < nfPrev) Fv = __fmaf_rn(__int_as_float(flips[t].y), gv[t], Fv);
+
+            // decide the batch in rounds
+            unsigned pending = __ballot_sync(FULL, valid), accBits = 0;
+            float d = 0.f;
+            while (pending) {
+                const bool mine = ((pending & ~blocked) >> lane) & 1u;
                 int acc = 0;
-                float d = 0.f;
-                if (lane == i) {
-                    float qyx = qs[x];
-                    float dE = sa ? dense_sa_dE(qyx, hx, Fv)
-                                  : dense_sqa_dE(qyx, hx, Fv, qn[0], qn[1], sc.twoDivM, sc.coef);
+                if (mine) {
+                    float qn0 = qb0 ? 1.f : -1.f, qn1 = qb1 ? 1.f : -1.f;
+                    if (nNbr == 1) qn1 = qn0;
+                    const float dE = sa ? dense_sa_dE(qx, hx, Fv)
+                                        : dense_sqa_dE(qx, hx, Fv, qn0, qn1, sc.twoDivM, sc.coef);
                     acc = metropolis(dE, sc.rate, u);
-                    if (acc) {
-                        qs[x] = (int8_t)(-qyx);
-                        d = -2.f * qyx;
-                        flips[nf] = make_int2(x, __float_as_int(d));
-                        if (T.trace) {
-                            uint32_t bitIdx = (uint32_t)k * (uint32_t)m + (uint32_t)y;
-                            atomicOr(&T.trace[(size_t)s * wordsPerStep + (bitIdx >> 5)], 1u << (bitIdx & 31));
-                        }
+                }
+                const unsigned accM = __ballot_sync(FULL, acc) & pending;
+                const unsigned blkM = blocked & pending;
+                const int fa = accM ? __ffs(accM) - 1 : 32;
+                const int fb = blkM ? __ffs(blkM) - 1 : 32;
+                if (fb < fa) {
+                    // undecided lanes below fb reject; fb waits for its neighbour trials
+                    pending &= ~((1u << fb) - 1u);
+                    if (lane == 0) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fb, accBits));
+                    const int w0 = __shfl_sync(FULL, nd0, fb), w1 = __shfl_sync(FULL, nd1, fb);
+                    unsigned long long av = 0;
+                    if (!wait_until([&] {
+                            av = uniform_acquire64(&S.logAvail);
+                            return avail_of(av, 0) > w0 && (nNbr < 2 || avail_of(av, 1) > w1);
+                        })) {
+                        aborted = true;
+                        break;
+                    }
+                    // re-evaluate every blocked lane (the ghost rows and A are unchanged)
+                    if ((blocked >> lane) & 1u) {
+                        bool known = nbr_bit(x, g0 + lane - 1 + before0, A0, avail_of(av, 0), ghost, lastJ, cnt,
+                                             ring, nlog, qb0, nd0);
+                        if (nNbr > 1)
+                            known &= nbr_bit(x, g0 + lane - 1 + before1, A1, avail_of(av, 1), ghost + ghostStride,
+                                             lastJ + kHash, cnt + kHash, ring + kRing, nlog + kLogWords, qb1, nd1);
+                        if (known) blocked &= ~(1u << lane);
+                    }
+                    blocked = __ballot_sync(FULL, (blocked >> lane) & 1u) & pending;
+                    continue;
+                }
+                if (fa == 32) break;  // every undecided lane rejects
+                // undecided lanes below fa reject; fa flips
+                const int xf = __shfl_sync(FULL, x, fa);
+                const float df = -2.f * __shfl_sync(FULL, qx, fa);
+                if (lane == fa) {
+                    qs[x] = (int8_t)(qx > 0.f ? -1 : 1);
+                    d = df;
+                    if (T.trace) {
+                        const int s = (g0 + lane) / N, k = g0 + lane - s * N;
+                        uint32_t bitIdx = (uint32_t)k * (uint32_t)m + (uint32_t)y;
+                        atomicOr(&T.trace[(size_t)s * wordsPerStep + (bitIdx >> 5)], 1u << (bitIdx & 31));
                     }
                 }
-                acc = __shfl_sync(FULL, acc, i);
-                if (acc) {
-                    d = __shfl_sync(FULL, d, i);
-                    if (lane > i) Fv = __fmaf_rn(d, Jgs[lane * 33 + i], Fv);
-                    accBits |= 1u << i;
-                    ++nf;
+                if (lane > fa) {
+                    Fv = __fmaf_rn(df, jg[fa], Fv);
+                    if (x == xf) qx = -qx;
                 }
+                accBits |= 1u << fa;
+                pending &= ~((2u << fa) - 1u);
+                // trials through fa are decided: make them visible to the neighbours
+                if (lane == 0 && pending) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
             }
             if (aborted) break;
-            accepted += (unsigned long long)nf;
-            if (lane == 0) {
-                __stcg(outLog + (size_t)y * nWords + (g0 >> 5), accBits);
-                st_release_gpu(progress + (size_t)y * kProgStride, (unsigned)(g0 + nValid));
-                S.nflip = nf;
-            }
             __syncwarp();
-            named_bar(1, 32 + kMcUpdaters);  // flips ready
+            if (lane == 0) {
+                S.decDone = b + 1;  // this batch's buffer is free
+                st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, nValid, accBits));
+            }
+            const int nf = __popc(accBits);
+            accepted += (unsigned long long)nf;
+
+            // the next batch's sites
+            const bool more = b + 1 < nBatches;
+            // (while waiting, keep applying published neighbour trials of this and
+            // earlier batches: the prefetcher may need those ring slots)
+            if (more && !wait_until([&] {
+                    if (nNbr > 0) apply_nbr(g0 + 32, g0 + 32);
+                    return uniform_acquire(&S.readyTag[(b + 1) & (kPre - 1)]) == b + 2;
+                })) {
+                aborted = true;
+                break;
+            }
+            const int xN = more ? preX[((b + 1) & (kPre - 1)) * 32 + lane] : 0;
+            const bool validN = g0 + 32 + lane < Itot;
+            // the next batch's fields start from the resident row once the updaters
+            // are done with the previous batch's flips; this batch's flips are
+            // gathered now and added after the next batch's neighbour work
+            const bool defer = nf <= kGv;
+            if (defer) {
+                unsigned rem = accBits;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) Jgs[lane * 33 + i] = Jn[i];
+                for (int t = 0; t < kGv; ++t) {
+                    if (rem) {
+                        const int f = __ffs(rem) - 1;
+                        rem &= rem - 1u;
+                        const int xf = __shfl_sync(FULL, x, f);
+                        gv[t] = validN ? __ldg(T.J + (size_t)xf * T.ldJ + xN) : 0.f;
+                    }
+                }
+            }
+            bar_sync(2, kBarCount);
+            float FvN = validN ? Fs[xN] : 0.f;
+            if ((accBits >> lane) & 1u) flips[__popc(accBits & ((1u << lane) - 1u))] = make_int2(x, __float_as_int(d));
+            if (lane == 0) S.nflip = nf;
+            __syncwarp();
+            __threadfence_block();
+            bar_arrive(1, kBarCount);
+            nfPrev = defer ? nf : 0;
+            if (!defer) {
+                // many flips: add them all now, in trial order
+                unsigned rem = accBits;
+                while (rem) {
+                    const int f = __ffs(rem) - 1;
+                    rem &= rem - 1u;
+                    const int xf = __shfl_sync(FULL, x, f);
+                    const float df = __shfl_sync(FULL, d, f);
+                    if (validN) FvN = __fmaf_rn(df, __ldg(T.J + (size_t)xf * T.ldJ + xN), FvN);
+                }
+            }
             x = xN;
-            u = uN;
-            sc = scN;
-            s = sN;
-            k = kN;
-            named_bar(2, 32 + kMcUpdaters);  // fields updated
+            Fv = FvN;
         }
+        bar_sync(2, kBarCount);  // the updaters are done with the last flips
         if (lane == 0) {
             if (aborted && T.status) atomicExch(T.status, (int)kErrTimeout);
             if (T.accepted) atomicAdd(T.accepted, accepted);
@@ -265,53 +452,134 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
             S.done = 1;
         }
         __syncwarp();
-        named_bar(1, 32 + kMcUpdaters);
+        __threadfence_block();
+        bar_arrive(1, kBarCount);
     } else if (warp == 1) {
-        // ------------------------------------------------------------- helper
-        while (nNbr > 0 && !S.done) {
-            for (int n = 0; n < nNbr; ++n) {
-                const int nb = n ? nbr1 : nbr0;
-                const int a = S.applied[n];
-                int head = S.ringHead[n];
-                const int lim = min(a + kRing, Itot);
-                if (head < lim) {
-                    int j = head + lane;
-                    if (j < lim) {
-                        int sj = j / N, kj = j - sj * N;
-                        u32x4 r = draw(T.seed, (uint32_t)kj, (uint32_t)nb, T.step0 + (uint32_t)sj, tag);
-                        ring[n * kRing + (j & (kRing - 1))] = draw_index(r.x, N);
-                    }
-                    __syncwarp();
-                    __threadfence_block();
-                    head = min(head + 32, lim);
-                    if (lane == 0) S.ringHead[n] = head;
-                    __syncwarp();
+        // -------------------------------------------------------------- helper
+        // lane l < 4 polls word (avail[n] >> 5) + dw of neighbour n = l & 1, dw = l >> 1
+        int avail0 = 0, avail1 = 0;
+        const int n = lane & 1, dw = lane >> 1;
+        const unsigned long long *nbLog = outLog + (size_t)(n ? nbr1 : nbr0) * nWords;
+        while (nNbr > 0 && !__shfl_sync(FULL, (int)S.done, 0)) {
+            const int an = n ? avail1 : avail0;
+            const int w = (an >> 5) + dw;
+            unsigned long long v = 0;
+            if (lane < 4 && n < nNbr && w * 32 < Itot && w < (S.applied[n] >> 5) + kLogWords)
+                v = ld_relaxed_u64(nbLog + w);
+            bool moved = false;
+#pragma unroll
+            for (int nn = 0; nn < 2; ++nn) {
+                int &a = nn ? avail1 : avail0;
+#pragma unroll
+                for (int ww = 0; ww < 2; ++ww) {
+                    const unsigned long long vv = __shfl_sync(FULL, v, nn + 2 * ww);
+                    const int wv = __shfl_sync(FULL, w, nn + 2 * ww);
+                    // words are consumed in order: the second only after the first is complete
+                    if (nn >= nNbr || wv != (a >> 5) || (int)(vv >> 38) != wv + 1) break;
+                    const int c = (int)((vv >> 32) & 63u);
+                    if (wv * 32 + c <= a) break;
+                    if (lane == 0) nlog[nn * kLogWords + (wv & (kLogWords - 1))] = (uint32_t)vv;
+                    a = wv * 32 + c;
+                    moved = true;
+                    if (c < min(32, Itot - wv * 32)) break;  // batch still being decided
                 }
-                const unsigned P = ld_acquire_gpu(progress + (size_t)nb * kProgStride);
-                const int cnt = min(min((int)P - a, 32), head - a);
-                if (cnt > 0) {
-                    const int j = a + lane;
-                    if (lane < cnt) {
-                        uint32_t w = __ldcg(outLog + (size_t)nb * nWords + (j >> 5));
-                        if ((w >> (j & 31)) & 1u) {
-                            int site = ring[n * kRing + (j & (kRing - 1))];
-                            atomicXor(&ghost[n * nWG + (site >> 5)], 1u << (site & 31));
-                        }
+            }
+            if (moved) {
+                __syncwarp();
+                if (lane == 0)
+                    st_release_cta64(&S.logAvail, (unsigned long long)(unsigned)avail0 |
+                                                      ((unsigned long long)(unsigned)avail1 << 32));
+            }
+        }
+    } else if (warp < kUpdWarp0) {
+        // --------------------------------------------------------- prefetchers
+        const int pw = warp - 2;
+        int s = 0, k = lane + 32 * pw, cs = -1;
+        while (k >= N) {
+            k -= N;
+            ++s;
+        }
+        StepConst sc = {0.f, 0.f, 0.f};
+        for (int p = pw; p < nBatches; p += kPf) {
+            // buffer p % kPre is free once the decider has finished batch p - kPre,
+            // and ring slots j - kRing are applied for the neighbours' iterations j of batch p
+            const int jEnd = 32 * p + 32;
+            int stop = 0;
+            if (!wait_until([&] {
+                    int ok = 0;
+                    if (lane == 0) {
+                        stop = S.done;
+                        ok = stop || (S.decDone > p - kPre && (nNbr < 1 || S.applied[0] + kRing >= jEnd) &&
+                                      (nNbr < 2 || S.applied[1] + kRing >= jEnd));
                     }
-                    __syncwarp();
-                    __threadfence_block();
-                    if (lane == 0) S.applied[n] = a + cnt;
-                    __syncwarp();
+                    return __shfl_sync(FULL, ok, 0) != 0;
+                }))
+                break;
+            if (__shfl_sync(FULL, stop, 0)) break;
+            __threadfence_block();
+            const int buf = p & (kPre - 1);
+            const int j = 32 * p + lane;
+            const bool valid = j < Itot;
+            int x = 0;
+            float u = 0.f;
+            if (valid) {
+                u32x4 r = draw(T.seed, (uint32_t)k, (uint32_t)y, T.step0 + (uint32_t)s, tag);
+                x = draw_index(r.x, N);
+                u = draw_unit(r.y);
+                if (s != cs) {
+                    const float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
+                    sc = step_const(T.algo, m, G, beta);
+                    cs = s;
                 }
+            }
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const int xi = __shfl_sync(FULL, x, i);
+                v[i] = (i < lane && valid) ? __ldg(T.J + (size_t)xi * T.ldJ + x) : 0.f;
+            }
+            // the neighbours' sites of the same iterations (while the gathers are in flight)
+            int site0 = 0, site1 = 0;
+            if (valid && nNbr > 0) {
+                site0 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr0, T.step0 + (uint32_t)s, tag).x, N);
+                ring[j & (kRing - 1)] = site0;
+                atomicAdd(&cnt[site0 & (kHash - 1)], 1);
+                if (nNbr > 1) {
+                    site1 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr1, T.step0 + (uint32_t)s, tag).x, N);
+                    ring[kRing + (j & (kRing - 1))] = site1;
+                    atomicAdd(&cnt[kHash + (site1 & (kHash - 1))], 1);
+                }
+            }
+            __syncwarp();
+            __threadfence_block();  // counts before last-trial entries
+            if (valid && nNbr > 0) {
+                atomicMax(&lastJ[site0 & (kHash - 1)], j);
+                if (nNbr > 1) atomicMax(&lastJ[kHash + (site1 & (kHash - 1))], j);
+            }
+            float *jg = Jg + buf * kJgStride + lane * 33;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) jg[i] = v[i];
+            preX[buf * 32 + lane] = x;
+            preU[buf * 32 + lane] = u;
+            preC[buf * 96 + lane] = sc.twoDivM;
+            preC[buf * 96 + 32 + lane] = sc.coef;
+            preC[buf * 96 + 64 + lane] = sc.rate;
+            __syncwarp();
+            if (lane == 0) st_release_cta(&S.readyTag[buf], p + 1);
+            k += 32 * kPf;
+            while (k >= N) {
+                k -= N;
+                ++s;
             }
         }
     } else {
         // ----------------------------------------------------------- updaters
-        const int ut = tid - 64;
+        const int ut = tid - 32 * kUpdWarp0;
         const int n4 = N / 4;
         float4 *F4 = reinterpret_cast<float4 *>(Fs);
+        bar_arrive(2, kBarCount);
         for (;;) {
-            named_bar(1, 32 + kMcUpdaters);
+            bar_sync(1, kBarCount);
             const int nf = S.nflip;
             if (nf < 0) break;
             for (int c0 = ut; c0 < n4; c0 += 4 * kMcUpdaters) {
@@ -343,7 +611,8 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
                     if (c < n4) F4[c] = f[t];
                 }
             }
-            named_bar(2, 32 + kMcUpdaters);
+            __threadfence_block();
+            bar_arrive(2, kBarCount);
         }
     }
     __syncthreads();
@@ -354,8 +623,9 @@ __global__ void __launch_bounds__(kMcThreads) dense_sweep_multi(sq103_dense_task
 }
 
 static size_t multi_smem_bytes(int N) {
-    int nWG = (N + 31) / 32;
-    return (size_t)N * 4 * 2 + 32 * 33 * 4 + (size_t)2 * nWG * 4 + 2 * kRing * 4 + 32 * 8 + (size_t)N + 16;
+    size_t ghostStride = (size_t)((N + 31) / 32 + 1) & ~(size_t)1;
+    return (size_t)N * 4 * 2 + (size_t)kPre * (kJgStride + 32 + 96 + 32) * 4 + 2 * ghostStride * 4 +
+           (size_t)2 * kHash * 4 * 2 + 2 * kRing * 4 + 2 * kLogWords * 4 + 32 * 8 + (size_t)N + 16;
 }
 
 static int multi_capacity(int N) {
@@ -374,7 +644,10 @@ static int multi_capacity(int N) {
         cudaGetLastError();
         return 0;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_sweep_multi, kMcThreads, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_sweep_multi, kMcThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     cachedN = N;
     cachedCap = perSm * sms;
     return cachedCap;
@@ -388,7 +661,7 @@ extern "C" {
 
 SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps) {
     unsigned long long nWords = ((unsigned long long)nSteps * N + 31) / 32;
-    return (unsigned long long)m * kProgStride * 4 + (unsigned long long)m * nWords * 4 + 256;
+    return (unsigned long long)m * nWords * 8 + 256;
 }
 
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo) {
@@ -403,14 +676,14 @@ int sq103_dense_anneal_multi(const sq103_dense_task *t, void *stream) {
     const int N = t->N, m = t->m;
     if ((long long)t->nSteps * N >= (1ll << 31)) return kErrBadShape;
     if (!t->ws || t->wsBytes < sq103_dense_ws_bytes(N, m, t->nSteps)) return kErrCapacity;
-    unsigned *progress = reinterpret_cast<unsigned *>(t->ws);
-    uint32_t *outLog = reinterpret_cast<uint32_t *>(progress + (size_t)m * kProgStride);
-    int nWords = (int)(((long long)t->nSteps * N + 31) / 32);
-    cudaError_t e = cudaMemsetAsync(progress, 0, (size_t)m * kProgStride * 4, st);
-    if (e != cudaSuccess) return (int)e;
     if (multi_capacity(N) < m) return kErrCapacity;
+    unsigned long long *outLog = reinterpret_cast<unsigned long long *>(t->ws);
+    int nWords = (int)(((long long)t->nSteps * N + 31) / 32);
+    // the accept words carry their batch tag; zero means "not published"
+    cudaError_t e = cudaMemsetAsync(outLog, 0, (size_t)m * nWords * 8, st);
+    if (e != cudaSuccess) return (int)e;
     sq103_dense_task task = *t;
-    void *args[] = {&task, &outLog, &progress, &nWords};
+    void *args[] = {&task, &outLog, &nWords};
     e = cudaLaunchCooperativeKernel((const void *)dense_sweep_multi, dim3(m), dim3(kMcThreads), args,
                                     multi_smem_bytes(N), st);
     return (int)e;

@@ -218,6 +218,28 @@ def test_dense_multi_cta_equals_single_cta(sq, algo, N, m):
     assert np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("N,m", [(4096, 256), (2048, 131)])
+def test_dense_multi_cta_equals_single_cta_large(sq, N, m):
+    """The benchmark shape (and an odd trotter count): trotters drift apart far
+    more at large N, so the neighbour synchronisation is exercised beyond the
+    lock-step regime of the small shapes.  Bit-identical to one CTA."""
+    rng = np.random.default_rng(N + m)
+    W = rand_sym(rng, N)
+    G = np.array([5.0, 0.9, 0.2, 0.05], np.float32)
+    out = []
+    for flags in (1, 2):
+        a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm="coloring")
+        a.set_kernel(flags)
+        a.seed(3)
+        a.prepare()
+        a.randomize_spin()
+        a.anneal(G, 50.0)
+        out.append((np.array(a.get_q()), a.get_E64(), a.get_accepted()))
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 @pytest.mark.parametrize("algo", ["coloring", "sa_naive"])
 def test_dense_multi_cta_replays_fp64(sq, orc, algo):
     N, m = 160, 9
