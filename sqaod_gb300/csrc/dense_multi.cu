@@ -27,19 +27,19 @@
 //           memory.
 //   warps 2-3 prefetchers, alternate batches: this trotter's own sites,
 //           uniforms and step constants, the in-batch gathers J[x_j][x_i]
-//           (j < i), and the neighbours' sites of the same iterations (a ring
-//           of sites, a count table hashed site -> neighbour trials not yet
-//           applied, and a last-trial table hashed site -> latest such trial),
-//           into a ring of kPre batch buffers with a ready tag each.
+//           (j < i) for the lanes j predicted to accept, the neighbours' sites of the same iterations (a ring of
+//           sites and one hashed-site bitmap per batch), and per lane the
+//           neighbour iterations of this and the previous batch that hit its
+//           site, into a ring of kPre batch buffers with a ready tag each.
 //   warps 4-7 updaters: F[y][:] += d * J[x][:] for the flips of the previous
 //           batch, in trial order, while the decider works on the next one.
 // Colour order: trial (y, k) must see neighbour n after every neighbour trial
 // that precedes it (iteration < k, or = k when n's colour phase comes first:
 // even trotters, then trotter m-1 if m is odd, then odd trotters).  The
 // decider applies neighbour flips to a ghost bit row of n only up to the
-// first trial of its current batch; each lane corrects its site for the
-// neighbour trials between that point and its own limit, which the count
-// table shows to be none for almost every lane.  A lane waits only when such
+// first trial of its current batch; each lane's bit is corrected for the
+// neighbour trials between that point and the lane's own limit, which the
+// prefetched lists show to be none for almost every lane.  A lane waits only when such
 // a neighbour trial is not yet published.  Every wait is bounded (global
 // timer) and ends the kernel with a timeout status instead of hanging; before
 // waiting a CTA publishes the trials it has decided, so waits always point to
@@ -58,10 +58,15 @@ constexpr int kMcUpdaters = kMcThreads - 32 * kUpdWarp0;
 constexpr int kBarCount = 32 + kMcUpdaters;       // decider + updaters
 constexpr int kRing = 256;      // neighbour sites kept per neighbour (power of two)
 constexpr int kLogWords = 32;   // neighbour accept words kept per neighbour (power of two)
-constexpr int kHash = 2048;     // count / last-trial table entries per neighbour (power of two)
+constexpr int kBmBits = 2048;   // bits of a batch's neighbour-site bitmap (hashed sites, power of two)
+constexpr int kBmWords = kBmBits / 32;
+constexpr int kBmSlots = kRing / 32;  // bitmaps kept per neighbour (one per ring batch)
 constexpr int kPre = 4;         // prefetched batches (power of two)
 constexpr int kJgStride = 32 * 33;
 constexpr int kGv = 16;         // flips of a batch whose gathers are deferred to the next batch
+constexpr int kCand = 2;        // neighbour iterations per lane and batch found by the prefetchers
+constexpr int kPredRows = 8;    // predicted accepting lanes whose gathers are kept in registers
+constexpr float kFieldDrift = 1.f;  // assumed field change between prefetch and decision
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -143,40 +148,44 @@ __device__ __forceinline__ bool wait_until(F &&ready) {
     return true;
 }
 
-// Neighbour spin bit at site x as of neighbour iteration Ji, from the ghost row
-// (iterations < A applied) and the published accept bits of iterations [A, Ji]
-// that hit x.  cnt[h] counts the neighbour iterations since A whose site hashes
-// to h and lastJ[h] is the latest of them; the prefetchers raise cnt before
-// lastJ, and lastJ is read first here, so a count of one with lastJ outside
-// [A, Ji] means the only such iteration comes after Ji.  Returns false (need =
-// latest unpublished iteration at x) when the bit cannot be known yet.
-__device__ __forceinline__ bool nbr_bit(int x, int Ji, int A, int avail, const uint32_t *ghost,
-                                        const volatile int *lastJ, const volatile int *cnt,
-                                        const volatile int *ring, const volatile uint32_t *nlog, int &bit,
-                                        int &need) {
-    bit = (ghost[x >> 5] >> (x & 31)) & 1;
+// Warp-wide.  The spin bit of a neighbour at the lane's site x after its
+// iteration Ji, from `bit` (its value after every published iteration below
+// j0) and the iterations j in [j0, Ji] that hit x: published ones (j < avail)
+// flip it when accepted; need returns the latest unpublished one (-1: none).
+// The batch bitmaps flag the lanes whose hashed site an iteration of that
+// batch hit; one ballot per flagged lane over the batch's sites finds them.
+// j0 and pLast (the batch of the latest Ji) are warp-uniform; only `active`
+// lanes take part.
+__device__ __forceinline__ void window_bits(int x, int Ji, int j0, int pLast, int avail, bool active,
+                                            const uint32_t *bmn, const int *rg, const uint32_t *nl, int Itot,
+                                            int &bit, int &need) {
+    const int lane = threadIdx.x & 31;
+    const int hb = x & (kBmBits - 1);
     need = -1;
-    const int h = x & (kHash - 1);
-    const int jl = lastJ[h];
-    const int c = cnt[h];
-    if (c == 0) return true;
-    if (c == 1) {
-        if (jl < A || jl > Ji || ring[jl & (kRing - 1)] != x) return true;
-        if (jl < avail) {
-            bit ^= (nlog[(jl >> 5) & (kLogWords - 1)] >> (jl & 31)) & 1;
-            return true;
+    for (int p = j0 >> 5; p <= pLast; ++p) {
+        const int jlo = max(j0, 32 * p);
+        const bool hit = active && Ji >= jlo && ((bmn[(p & (kBmSlots - 1)) * kBmWords + (hb >> 5)] >> (hb & 31)) & 1u);
+        unsigned hits = __ballot_sync(FULL, hit);
+        if (!hits) continue;
+        const int jl = 32 * p + lane;
+        const int sj = jl < Itot ? rg[jl & (kRing - 1)] : -1;
+        const uint32_t accw = nl[p & (kLogWords - 1)];  // accept bits, valid below avail
+        while (hits) {
+            const int i = __ffs(hits) - 1;
+            hits &= hits - 1u;
+            const int xi = __shfl_sync(FULL, x, i), Jii = __shfl_sync(FULL, Ji, i);
+            const unsigned mt = __ballot_sync(FULL, sj == xi && jl >= jlo && jl <= Jii);
+            if (lane == i) {
+                for (unsigned r = mt; r; r &= r - 1u) {
+                    const int j = 32 * p + __ffs(r) - 1;
+                    if (j < avail)
+                        bit ^= (accw >> (j & 31)) & 1u;
+                    else
+                        need = j;
+                }
+            }
         }
-        need = jl;
-        return false;
     }
-    for (int j = A; j <= Ji; ++j) {
-        if (ring[j & (kRing - 1)] != x) continue;
-        if (j < avail)
-            bit ^= (nlog[(j >> 5) & (kLogWords - 1)] >> (j & 31)) & 1;
-        else
-            need = j;
-    }
-    return need < 0;
 }
 
 __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_task T, unsigned long long *outLog,
@@ -204,11 +213,12 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
     float *preC = preU + kPre * 32;                                     // kPre x 3 x 32
     int *preX = reinterpret_cast<int *>(preC + kPre * 96);              // kPre x 32
     uint32_t *ghost = reinterpret_cast<uint32_t *>(preX + kPre * 32);   // 2 x ghostStride
-    int *lastJ = reinterpret_cast<int *>(ghost + 2 * ghostStride);      // 2 x kHash
-    int *cnt = lastJ + 2 * kHash;                                       // 2 x kHash
-    int *ring = cnt + 2 * kHash;                                        // 2 x kRing
+    uint32_t *bm = ghost + 2 * ghostStride;                             // 2 x kBmSlots x kBmWords
+    int *ring = reinterpret_cast<int *>(bm + 2 * kBmSlots * kBmWords);  // 2 x kRing
     uint32_t *nlog = reinterpret_cast<uint32_t *>(ring + 2 * kRing);    // 2 x kLogWords
-    int2 *flips = reinterpret_cast<int2 *>(nlog + 2 * kLogWords);       // 32
+    int *cand = reinterpret_cast<int *>(nlog + 2 * kLogWords);          // kPre x 2 x kCand x 32
+    unsigned *prePred = reinterpret_cast<unsigned *>(cand + kPre * 2 * kCand * 32);  // kPre
+    int2 *flips = reinterpret_cast<int2 *>(prePred + kPre);             // 32
     int8_t *qs = reinterpret_cast<int8_t *>(flips + 32);                // N
 
     for (int i = tid; i < N; i += kMcThreads) {
@@ -223,10 +233,6 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
             for (int b = 0; b < 32 && w * 32 + b < N; ++b) bits |= (qn[w * 32 + b] > 0 ? 1u : 0u) << b;
             ghost[n * ghostStride + w] = bits;
         }
-    }
-    for (int i = tid; i < 2 * kHash; i += kMcThreads) {
-        lastJ[i] = -1;
-        cnt[i] = 0;
     }
     if (tid == 0) {
         S.logAvail = 0;
@@ -245,14 +251,17 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
         const uint32_t wordsPerStep = (uint32_t)(((size_t)N * m + 31) / 32);
         unsigned long long accepted = 0;
         bool aborted = false;
-        int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
         int nfPrev = 0;      // flips of the previous batch still to be added to Fv
+        int qb0 = 0, qb1 = 0, nd0 = -1, nd1 = -1;  // neighbour bits of the lane's site, unknown iterations
+        int x = 0;                                  // the lane's site in the current batch
         float gv[kGv];       // their gathers J[x_f][x] (at this batch's sites)
 #pragma unroll
         for (int t = 0; t < kGv; ++t) gv[t] = 0.f;
 
-        // Applies the published neighbour trials below lim0 / lim1 (their sites are in
-        // the ring) to the ghost rows; returns the helper's availability word.
+        int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
+
+        // Applies the published neighbour iterations below lim0 / lim1 (their sites
+        // are in the ring) to the ghost rows; returns the helper's availability word.
         auto apply_nbr = [&](int lim0, int lim1) {
             const unsigned long long av = uniform_acquire64(&S.logAvail);
             lim0 = min(avail_of(av, 0), lim0);
@@ -262,11 +271,10 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
 #pragma unroll
                 for (int n = 0; n < 2; ++n) {
                     const int j = (n ? A1 : A0) + j0 + lane;
-                    if (n < nNbr && j < (n ? lim1 : lim0)) {
+                    if (n < nNbr && j < (n ? lim1 : lim0) &&
+                        ((nlog[n * kLogWords + ((j >> 5) & (kLogWords - 1))] >> (j & 31)) & 1u)) {
                         const int site = ring[n * kRing + (j & (kRing - 1))];
-                        atomicSub(&cnt[n * kHash + (site & (kHash - 1))], 1);
-                        if ((nlog[n * kLogWords + ((j >> 5) & (kLogWords - 1))] >> (j & 31)) & 1u)
-                            atomicXor(&ghost[n * ghostStride + (site >> 5)], 1u << (site & 31));
+                        atomicXor(&ghost[n * ghostStride + (site >> 5)], 1u << (site & 31));
                     }
                 }
             }
@@ -282,8 +290,63 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
             return av;
         };
 
+        // Neighbour bits at the lane's site for batch b: the ghost row (iterations
+        // < A applied) corrected by the neighbour iterations in [A, Ji] at the site,
+        // which the prefetchers listed (the latest kCand of the last three batches).
+        // A neighbour more than two batches behind, or a longer list, takes the
+        // bitmap scan of window_bits.  need: latest unpublished such iteration (-1: none).
+        auto nbr_bits = [&](int b, int g0, bool valid, unsigned long long av) {
+            const int buf = b & (kPre - 1);
+            bool slow = false;
+#pragma unroll
+            for (int n = 0; n < 2; ++n) {
+                if (n >= nNbr) break;
+                const int A = n ? A1 : A0, avail = avail_of(av, n);
+                int bit = (ghost[n * ghostStride + (x >> 5)] >> (x & 31)) & 1, need = -1;
+                const int ca = cand[((buf * 2 + n) * kCand) * 32 + lane];
+                const int cb = cand[((buf * 2 + n) * kCand + 1) * 32 + lane];
+                slow |= ca == -2 || A < 32 * (b - 2);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const int j = c ? cb : ca;
+                    if (j >= A) {
+                        if (j < avail)
+                            bit ^= (nlog[n * kLogWords + ((j >> 5) & (kLogWords - 1))] >> (j & 31)) & 1u;
+                        else
+                            need = max(need, j);
+                    }
+                }
+                if (n) {
+                    qb1 = bit;
+                    nd1 = valid ? need : -1;
+                } else {
+                    qb0 = bit;
+                    nd0 = valid ? need : -1;
+                }
+            }
+            slow = slow && valid;
+            if (__any_sync(FULL, slow)) {
+#pragma unroll
+                for (int n = 0; n < 2; ++n) {
+                    if (n >= nNbr) break;
+                    int bit = (ghost[n * ghostStride + (x >> 5)] >> (x & 31)) & 1, need;
+                    window_bits(x, g0 + lane - 1 + (n ? before1 : before0), n ? A1 : A0, b, avail_of(av, n), slow,
+                                bm + n * kBmSlots * kBmWords, ring + n * kRing, nlog + n * kLogWords, Itot, bit, need);
+                    if (slow) {
+                        if (n) {
+                            qb1 = bit;
+                            nd1 = need;
+                        } else {
+                            qb0 = bit;
+                            nd0 = need;
+                        }
+                    }
+                }
+            }
+        };
+
         aborted = !wait_until([&] { return uniform_acquire(&S.readyTag[0]) == 1; });
-        int x = preX[lane];
+        x = preX[lane];
         float Fv = Fs[x];
 
         for (int b = 0; b < nBatches && !aborted; ++b) {
@@ -294,47 +357,53 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
             const float u = preU[buf * 32 + lane];
             const StepConst sc = {preC[buf * 96 + lane], preC[buf * 96 + 32 + lane], preC[buf * 96 + 64 + lane]};
             const float *jg = Jg + buf * kJgStride + lane * 33;
+            const unsigned pred = prePred[buf];  // lanes whose row of in-batch gathers is in jg
             const float hx = valid ? hs[x] : 0.f;
             float qx = valid ? (float)qs[x] : 1.f;
 
             // neighbour spins at this batch's sites: apply the published neighbour
-            // trials before this batch's first trial (both neighbours in one pass;
-            // their sites are in the ring since this batch's buffer is ready)
-            int qb0 = 0, qb1 = 0, nd0 = -1, nd1 = -1;
+            // iterations before this batch's first trial (their sites are in the ring
+            // since this batch's buffer is ready), then correct each lane's site
+            qb0 = qb1 = 0;
+            nd0 = nd1 = -1;
             unsigned blocked = 0;
             if (nNbr > 0) {
                 const unsigned long long av = apply_nbr(g0 + before0, g0 + before1);
-                if (valid) {
-                    bool known = nbr_bit(x, g0 + lane - 1 + before0, A0, avail_of(av, 0), ghost, lastJ, cnt, ring,
-                                         nlog, qb0, nd0);
-                    if (nNbr > 1)
-                        known &= nbr_bit(x, g0 + lane - 1 + before1, A1, avail_of(av, 1), ghost + ghostStride,
-                                         lastJ + kHash, cnt + kHash, ring + kRing, nlog + kLogWords, qb1, nd1);
-                    if (!known) blocked = 1u << lane;
-                }
-                blocked = __reduce_or_sync(FULL, blocked);
+                nbr_bits(b, g0, valid, av);
+                blocked = __ballot_sync(FULL, nd0 >= 0 || nd1 >= 0);
             }
 
             // the previous batch's flips (gathered at the end of that batch)
 #pragma unroll
-            for (int t = 0; t < kGv; ++t)
-                if (t < nfPrev) Fv = __fmaf_rn(__int_as_float(flips[t].y), gv[t], Fv);
+            for (int t = 0; t < kGv; ++t) {
+                if (t >= nfPrev) break;
+                Fv = __fmaf_rn(__int_as_float(flips[t].y), gv[t], Fv);
+            }
 
             // decide the batch in rounds
             unsigned pending = __ballot_sync(FULL, valid), accBits = 0;
             float d = 0.f;
             while (pending) {
-                const bool mine = ((pending & ~blocked) >> lane) & 1u;
-                int acc = 0;
-                if (mine) {
-                    float qn0 = qb0 ? 1.f : -1.f, qn1 = qb1 ? 1.f : -1.f;
-                    if (nNbr == 1) qn1 = qn0;
-                    const float dE = sa ? dense_sa_dE(qx, hx, Fv)
-                                        : dense_sqa_dE(qx, hx, Fv, qn0, qn1, sc.twoDivM, sc.coef);
-                    acc = metropolis(dE, sc.rate, u);
+                // a lane with unknown neighbour bits is decided anyway when every value
+                // those bits can take gives the same outcome; it blocks otherwise
+                int acc = 0, amb = 0;
+                if ((pending >> lane) & 1u) {
+                    const float qn0 = qb0 ? 1.f : -1.f, qn1 = nNbr == 1 ? qn0 : (qb1 ? 1.f : -1.f);
+                    auto accept = [&](float a, float c) {
+                        const float dE = sa ? dense_sa_dE(qx, hx, Fv)
+                                            : dense_sqa_dE(qx, hx, Fv, a, c, sc.twoDivM, sc.coef);
+                        return (int)metropolis(dE, sc.rate, u);
+                    };
+                    acc = accept(qn0, qn1);
+                    if ((blocked >> lane) & 1u) {
+                        const bool u0 = nd0 >= 0, u1 = nNbr > 1 && nd1 >= 0;
+                        if (u0 && accept(-qn0, nNbr == 1 ? -qn0 : qn1) != acc) amb = 1;
+                        if (u1 && accept(qn0, -qn1) != acc) amb = 1;
+                        if (u0 && u1 && accept(-qn0, -qn1) != acc) amb = 1;
+                    }
                 }
-                const unsigned accM = __ballot_sync(FULL, acc) & pending;
-                const unsigned blkM = blocked & pending;
+                const unsigned accM = __ballot_sync(FULL, acc && !amb) & pending;
+                const unsigned blkM = __ballot_sync(FULL, amb) & pending;
                 const int fa = accM ? __ffs(accM) - 1 : 32;
                 const int fb = blkM ? __ffs(blkM) - 1 : 32;
                 if (fb < fa) {
@@ -350,16 +419,9 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
                         aborted = true;
                         break;
                     }
-                    // re-evaluate every blocked lane (the ghost rows and A are unchanged)
-                    if ((blocked >> lane) & 1u) {
-                        bool known = nbr_bit(x, g0 + lane - 1 + before0, A0, avail_of(av, 0), ghost, lastJ, cnt,
-                                             ring, nlog, qb0, nd0);
-                        if (nNbr > 1)
-                            known &= nbr_bit(x, g0 + lane - 1 + before1, A1, avail_of(av, 1), ghost + ghostStride,
-                                             lastJ + kHash, cnt + kHash, ring + kRing, nlog + kLogWords, qb1, nd1);
-                        if (known) blocked &= ~(1u << lane);
-                    }
-                    blocked = __ballot_sync(FULL, (blocked >> lane) & 1u) & pending;
+                    // re-evaluate (the ghost rows and A are unchanged within the batch)
+                    nbr_bits(b, g0, valid, av);
+                    blocked = __ballot_sync(FULL, nd0 >= 0 || nd1 >= 0) & pending;
                     continue;
                 }
                 if (fa == 32) break;  // every undecided lane rejects
@@ -376,7 +438,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
                     }
                 }
                 if (lane > fa) {
-                    Fv = __fmaf_rn(df, jg[fa], Fv);
+                    const float jv = ((pred >> fa) & 1u) ? jg[fa] : __ldg(T.J + (size_t)xf * T.ldJ + x);
+                    Fv = __fmaf_rn(df, jv, Fv);
                     if (x == xf) qx = -qx;
                 }
                 accBits |= 1u << fa;
@@ -395,11 +458,12 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
 
             // the next batch's sites
             const bool more = b + 1 < nBatches;
-            // (while waiting, keep applying published neighbour trials of this and
-            // earlier batches: the prefetcher may need those ring slots)
+            // (while waiting, keep applying published neighbour iterations of this and
+            // earlier batches: the prefetchers may need those ring slots)
             if (more && !wait_until([&] {
+                    if (uniform_acquire(&S.readyTag[(b + 1) & (kPre - 1)]) == b + 2) return true;
                     if (nNbr > 0) apply_nbr(g0 + 32, g0 + 32);
-                    return uniform_acquire(&S.readyTag[(b + 1) & (kPre - 1)]) == b + 2;
+                    return false;
                 })) {
                 aborted = true;
                 break;
@@ -410,16 +474,14 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
             // are done with the previous batch's flips; this batch's flips are
             // gathered now and added after the next batch's neighbour work
             const bool defer = nf <= kGv;
-            if (defer) {
+            if (defer && accBits) {
                 unsigned rem = accBits;
 #pragma unroll
                 for (int t = 0; t < kGv; ++t) {
-                    if (rem) {
-                        const int f = __ffs(rem) - 1;
-                        rem &= rem - 1u;
-                        const int xf = __shfl_sync(FULL, x, f);
-                        gv[t] = validN ? __ldg(T.J + (size_t)xf * T.ldJ + xN) : 0.f;
-                    }
+                    const int xf = __shfl_sync(FULL, x, __ffs(rem) - 1);
+                    gv[t] = validN ? __ldg(T.J + (size_t)xf * T.ldJ + xN) : 0.f;
+                    rem &= rem - 1u;
+                    if (!rem) break;
                 }
             }
             bar_sync(2, kBarCount);
@@ -532,33 +594,125 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
                     cs = s;
                 }
             }
-            float v[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const int xi = __shfl_sync(FULL, x, i);
-                v[i] = (i < lane && valid) ? __ldg(T.J + (size_t)xi * T.ldJ + x) : 0.f;
+            // the in-batch gathers J[x_f][x_i] (i > f) are needed only for the lanes f
+            // that accept: predict them from the current (a few batches stale) field,
+            // spins and ghost rows with a margin for the drift; the decider gathers
+            // the row of an accepting lane that was not predicted itself
+            unsigned pred;
+            {
+                const volatile float *vF = Fs, *vh = hs;
+                const volatile int8_t *vq = qs;
+                const volatile uint32_t *vg = ghost;
+                const float qx = (float)vq[x], hx = vh[x], fx = vF[x];
+                float qn0 = ((vg[x >> 5] >> (x & 31)) & 1u) ? 1.f : -1.f;
+                float qn1 = nNbr > 1 ? (((vg[ghostStride + (x >> 5)] >> (x & 31)) & 1u) ? 1.f : -1.f) : qn0;
+                const float dE = sa ? dense_sa_dE(qx, hx, fx) : dense_sqa_dE(qx, hx, fx, qn0, qn1, sc.twoDivM, sc.coef);
+                const float margin = (sa ? 4.f : 2.f * sc.twoDivM) * kFieldDrift;
+                pred = __ballot_sync(FULL, valid && metropolis(dE - margin, sc.rate, u));
             }
-            // the neighbours' sites of the same iterations (while the gathers are in flight)
-            int site0 = 0, site1 = 0;
-            if (valid && nNbr > 0) {
-                site0 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr0, T.step0 + (uint32_t)s, tag).x, N);
-                ring[j & (kRing - 1)] = site0;
-                atomicAdd(&cnt[site0 & (kHash - 1)], 1);
-                if (nNbr > 1) {
-                    site1 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr1, T.step0 + (uint32_t)s, tag).x, N);
-                    ring[kRing + (j & (kRing - 1))] = site1;
-                    atomicAdd(&cnt[kHash + (site1 & (kHash - 1))], 1);
+            float v[kPredRows];
+            {
+                unsigned r = pred;
+#pragma unroll
+                for (int t = 0; t < kPredRows; ++t) {
+                    if (!r) break;
+                    const int f = __ffs(r) - 1;
+                    r &= r - 1u;
+                    const int xf = __shfl_sync(FULL, x, f);
+                    v[t] = (lane > f && valid) ? __ldg(T.J + (size_t)xf * T.ldJ + x) : 0.f;
                 }
             }
-            __syncwarp();
-            __threadfence_block();  // counts before last-trial entries
-            if (valid && nNbr > 0) {
-                atomicMax(&lastJ[site0 & (kHash - 1)], j);
-                if (nNbr > 1) atomicMax(&lastJ[kHash + (site1 & (kHash - 1))], j);
+            // the neighbours' sites of the same iterations (while the gathers are in
+            // flight): ring entries and the batch's site bitmaps; then, per lane and
+            // neighbour, the latest kCand iterations of batches p - 2 .. p that hit
+            // the lane's site up to its limit (-2: more than kCand)
+            if (nNbr > 0) {
+                uint32_t *bp = bm + (p & (kBmSlots - 1)) * kBmWords;
+                bp[lane] = 0u;
+                bp[lane + 32] = 0u;
+                if (nNbr > 1) {
+                    bp[kBmSlots * kBmWords + lane] = 0u;
+                    bp[kBmSlots * kBmWords + lane + 32] = 0u;
+                }
+                __syncwarp();
+                int cur0 = -1, cur1 = -1;
+                if (valid) {
+                    cur0 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr0, T.step0 + (uint32_t)s, tag).x, N);
+                    ring[j & (kRing - 1)] = cur0;
+                    atomicOr(&bp[(cur0 & (kBmBits - 1)) >> 5], 1u << (cur0 & 31));
+                    if (nNbr > 1) {
+                        cur1 = draw_index(draw(T.seed, (uint32_t)k, (uint32_t)nbr1, T.step0 + (uint32_t)s, tag).x, N);
+                        ring[kRing + (j & (kRing - 1))] = cur1;
+                        atomicOr(&bp[kBmSlots * kBmWords + ((cur1 & (kBmBits - 1)) >> 5)], 1u << (cur1 & 31));
+                    }
+                }
+                // batch p - 1 (the other prefetcher's) must be in the ring; its buffer
+                // slot may already hold a later batch (batch p - 2 is this warp's own)
+                if (p > 0 && !wait_until([&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
+                    break;
+                __syncwarp();
+                const int hb = x & (kBmBits - 1);
+#pragma unroll
+                for (int nn = 0; nn < 2; ++nn) {
+                    if (nn >= nNbr) break;
+                    const uint32_t *bmn = bm + nn * kBmSlots * kBmWords;
+                    const int prev = p > 0 ? ring[nn * kRing + ((32 * (p - 1) + lane) & (kRing - 1))] : -1;
+                    const int prev2 = p > 1 ? ring[nn * kRing + ((32 * (p - 2) + lane) & (kRing - 1))] : -1;
+                    const int cur = nn ? cur1 : cur0;
+                    const int lim = lane - 1 + (nn ? before1 : before0);  // latest iteration of batch p a lane needs
+                    auto marked = [&](int q) {
+                        return q >= 0 && ((bmn[(q & (kBmSlots - 1)) * kBmWords + (hb >> 5)] >> (hb & 31)) & 1u);
+                    };
+                    const bool flag = valid && (marked(p) || marked(p - 1) || marked(p - 2));
+                    int c0 = -1, c1 = -1;
+                    unsigned hits = __ballot_sync(FULL, flag);
+                    while (hits) {
+                        const int i = __ffs(hits) - 1;
+                        hits &= hits - 1u;
+                        const int xi = __shfl_sync(FULL, x, i), li = __shfl_sync(FULL, lim, i);
+                        const unsigned mc = __ballot_sync(FULL, cur == xi && lane <= li);
+                        const unsigned mp = __ballot_sync(FULL, prev == xi);
+                        const unsigned mq = __ballot_sync(FULL, prev2 == xi);
+                        if (lane == i) {
+                            if (__popc(mc) + __popc(mp) + __popc(mq) > kCand) {
+                                c0 = -2;
+                            } else {
+                                // the latest two: batch p first, then p - 1, then p - 2
+                                const unsigned ms[3] = {mc, mp, mq};
+#pragma unroll
+                                for (int q = 0; q < 3; ++q) {
+                                    for (unsigned r = ms[q]; r; r &= ~(1u << (31 - __clz(r)))) {
+                                        const int jj = 32 * (p - q) + 31 - __clz(r);
+                                        if (c0 < 0)
+                                            c0 = jj;
+                                        else
+                                            c1 = jj;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    cand[((buf * 2 + nn) * kCand) * 32 + lane] = c0;
+                    cand[((buf * 2 + nn) * kCand + 1) * 32 + lane] = c1;
+                }
             }
             float *jg = Jg + buf * kJgStride + lane * 33;
+            {
+                unsigned r = pred;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) jg[i] = v[i];
+                for (int t = 0; t < kPredRows; ++t) {
+                    if (!r) break;
+                    const int f = __ffs(r) - 1;
+                    r &= r - 1u;
+                    jg[f] = v[t];
+                }
+                for (; r; r &= r - 1u) {  // more predicted rows than registers: gather the rest here
+                    const int f = __ffs(r) - 1;
+                    const int xf = __shfl_sync(FULL, x, f);
+                    jg[f] = (lane > f && valid) ? __ldg(T.J + (size_t)xf * T.ldJ + x) : 0.f;
+                }
+            }
+            if (lane == 0) prePred[buf] = pred;
             preX[buf * 32 + lane] = x;
             preU[buf * 32 + lane] = u;
             preC[buf * 96 + lane] = sc.twoDivM;
@@ -625,7 +779,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
 static size_t multi_smem_bytes(int N) {
     size_t ghostStride = (size_t)((N + 31) / 32 + 1) & ~(size_t)1;
     return (size_t)N * 4 * 2 + (size_t)kPre * (kJgStride + 32 + 96 + 32) * 4 + 2 * ghostStride * 4 +
-           (size_t)2 * kHash * 4 * 2 + 2 * kRing * 4 + 2 * kLogWords * 4 + 32 * 8 + (size_t)N + 16;
+           (size_t)2 * kBmSlots * kBmWords * 4 + 2 * kRing * 4 + 2 * kLogWords * 4 + (size_t)kPre * 2 * kCand * 32 * 4 + kPre * 4 +
+           32 * 8 + (size_t)N + 16;
 }
 
 static int multi_capacity(int N) {
