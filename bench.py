@@ -13,8 +13,9 @@ acceptance mix matches a whole anneal.
            inputs resident in HBM, CUDA events on the launching stream,
            L2 flushed between timed steps with a 512 MB write)
   e2e    : the same metric through the solver-handle C ABI with host
-           buffers: set_qubo (H2D of W), seed, prepare, randomize_spin,
-           K annealOneStep calls, make_solution, get_E and get_x (D2H)
+           buffers, for one whole anneal as a user runs it: set_qubo (H2D of
+           W), seed, prepare, randomize_spin, anneal over the 619-step
+           schedule, make_solution, get_E and get_x (D2H)
   roofline: HBM roofline of the sweep kernel: algorithmic bytes per launch
            = A * 4N + 10 N m (A = accepted flips counted by the kernel)
   cpu_baseline: the reference CPU coloring annealer (restated with the
@@ -71,15 +72,71 @@ def peaks():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """Samples the SM clock and clock-event reasons while the timed region runs.
+
+    Reads NVML directly (libnvidia-ml, every 2 ms, on a thread) so that even a
+    timed region of a few tens of milliseconds is covered; falls back to
+    `nvidia-smi -lms 200`.  Read-only: no clock or other setting is changed.
+    """
+    # nvmlClocksEventReasons bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap", 0x80: "hw_power_brake_slowdown"}
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu):
         self.gpu, self.proc, self.path = gpu, None, None
+        self.samples, self.stop, self.thread, self.nvml, self.handle = [], False, None, None, None
+
+    def _nvml_open(self):
+        try:
+            import torch
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            uuid = getattr(torch.cuda.get_device_properties(self.gpu), "uuid", None)
+            ok = False
+            if uuid is not None:
+                u = str(uuid)
+                u = u if u.startswith("GPU-") else "GPU-" + u
+                ok = nv.nvmlDeviceGetHandleByUUID(u.encode(), ctypes.byref(h)) == 0
+            if not ok:
+                cnt = ctypes.c_uint()
+                if nv.nvmlDeviceGetCount_v2(ctypes.byref(cnt)) != 0 or cnt.value != 1:
+                    return False
+                ok = nv.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) == 0
+            if not ok:
+                return False
+            self.nvml, self.handle = nv, h
+            return True
+        except Exception:
+            return False
+
+    def _run(self):
+        nv, h = self.nvml, self.handle
+        mhz, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        get_reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop:
+            if (nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0 and
+                    nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and
+                    get_reasons(h, ctypes.byref(rs)) == 0):
+                self.samples.append((mhz.value, mx.value, rs.value))
+            time.sleep(0.002)
 
     def __enter__(self):
+        if self._nvml_open():
+            # the timed region is a tight loop of short host calls: let the
+            # sampling thread take the interpreter often
+            self.switch = sys.getswitchinterval()
+            sys.setswitchinterval(1e-4)
+            self.thread = threading.Thread(target=self._run, daemon=True)
+            self.thread.start()
+            while not self.samples and self.thread.is_alive():
+                time.sleep(0.001)
+            return self
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -91,6 +148,10 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
+        if self.thread:
+            self.stop = True
+            self.thread.join(1.0)
+            sys.setswitchinterval(self.switch)
         if self.proc:
             self.proc.terminate()
             try:
@@ -99,6 +160,17 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.thread:
+            if not self.samples:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "source": "nvml"}
+            reasons = set()
+            for _, _, r in self.samples:
+                for bit, name in self.REASONS.items():
+                    if r & bit:
+                        reasons.add(name)
+            return {"sm_mhz": statistics.median(s[0] for s in self.samples),
+                    "sm_max_mhz": max(s[1] for s in self.samples), "reasons": sorted(reasons),
+                    "samples": len(self.samples), "source": "nvml"}
         sm, mx, reasons = [], [], set()
         try:
             for line in open(self.path):
@@ -118,9 +190,9 @@ class ClockSampler:
         except OSError:
             pass
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "source": "nvidia-smi"}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi"}
 
 
 class DenseTask(ctypes.Structure):
@@ -178,6 +250,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default="%d,%d" % (N_SPINS, N_TROTTERS),
+                    help="N,m of the instance (smaller cases are for profiling captures only)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -200,7 +275,7 @@ def main():
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     dev = torch.device("cuda", local)
-    N, m = N_SPINS, N_TROTTERS
+    N, m = (int(v) for v in args.size.split(","))
     W = problem(N)
 
     def P(t):
@@ -278,47 +353,59 @@ def main():
     achieved_gbs = float(alg_bytes.sum()) / (t_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
-    # -------- end to end through the solver-handle C ABI with host buffers
+    # -------- end to end through the solver-handle C ABI with host buffers: one
+    # whole anneal of the 619-step schedule, as a user runs it (set_qubo uploads W,
+    # anneal runs the schedule, make_solution / get_E / get_x bring the result back)
     e2e = None
-    if rank == 0 or True:
+    if not args.no_e2e:
         Wh = np.ascontiguousarray(W)
+        G_all = np.array(sched, np.float32)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         ann = sq.cuda.dense_graph_annealer(Wh, sq.minimize, n_trotters=m, algorithm="coloring")
         ann.seed(seed)
         ann.prepare()
         ann.randomize_spin()
-        for i in range(K):
-            ann.anneal_one_step(sched[idx[i]], BETA)
+        t1 = time.perf_counter()
+        ann.anneal(G_all, BETA)
+        t2 = time.perf_counter()
         ann.make_solution()
         E = ann.get_E()
         x = ann.get_x()
         e2e_s = time.perf_counter() - t0
-        e2e = {"value": trials / e2e_s, "unit": "trials/s",
-               "h2d_bytes_per_step": int((Wh.nbytes + 8 * K) / K),
-               "d2h_bytes_per_step": int((m * N + 8 * m + 4 * len(E)) / K),
-               "min_E": float(np.min(E))}
+        phases = {"setup_s": t1 - t0, "anneal_s": t2 - t1, "solution_s": e2e_s - (t2 - t0)}
+        nS = len(G_all)
+        e2e = {"value": float(N) * m * nS / e2e_s, "unit": "trials/s",
+               "h2d_bytes_per_step": int((Wh.nbytes + G_all.nbytes * 2) / nS),
+               "d2h_bytes_per_step": int((m * N + 4 * len(E)) / nS),
+               "steps": nS, "seconds": e2e_s, "phases": phases, "min_E": float(np.min(E))}
         del ann, x
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and (N, m) == (N_SPINS, N_TROTTERS):
         val, cores, dt = cpu_reference(W, 1)
         cpu = {"value": val, "unit": "trials/s", "cores": cores, "kind": "port",
                "sample": "1 annealOneStep (1,048,576 trials) at G=5.0 of the same instance, %.1f s" % dt}
 
     if rank == 0:
-        line = {"metric": "spin-flip trials/s (dense SQA coloring, N=4096 m=256)", "value": value,
+        traffic = None
+        try:
+            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+                traffic = json.load(f).get("dense_sweep_multi N=%d m=%d" % (N, m), {}).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+        line = {"metric": "spin-flip trials/s (dense SQA coloring, N=%d m=%d)" % (N, m), "value": value,
                 "unit": "trials/s", "n_gpus": world, "steps": K, "warmup": Wm, "ms_per_step": t_ms / K,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (sqaod generate_random_symmetric_W(4096, -1, 1), np.random.seed(0))",
-                "config": {"workload": "dense SQA coloring N=4096 m=256 beta=50 G=5*0.99^k (619-step "
+                "data": "synthetic (sqaod generate_random_symmetric_W(%d, -1, 1), np.random.seed(0))" % N,
+                "config": {"workload": "dense SQA coloring N=%d m=%d beta=50 G=5*0.99^k (619-step " % (N, m) +
                                        "schedule sampled evenly over the timed steps)",
                            "N": N, "m": m, "algorithm": "coloring", "l2": "flushed between timed steps (512 MB write)",
                            "kernel": "one CTA per trotter (cooperative)" if multi else "one CTA per instance",
                            "parallelism": "replicas" if world > 1 else "single instance"},
                 "e2e": e2e, "gpu_launches": K,
                 "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
-                             "frac": achieved_gbs / peak, "traffic": None, "peak_source": peak_kind,
+                             "frac": achieved_gbs / peak, "traffic": traffic, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": float(alg_bytes.mean()),
                              "accepted_per_step": float(accepted.mean())},
                 "cpu_baseline": cpu, "clocks": clk.summary(), "wall_s": wall}

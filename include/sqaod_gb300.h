@@ -67,7 +67,9 @@ typedef struct sq103_dense_task {
     const float *h;       /* N */
     int8_t *q;            /* m x N spins, row stride N */
     float *F;             /* m x N local fields F[y][i] = sum_j J[i][j] q[y][j] */
-    uint32_t *trace;      /* optional: accept bits per step (layout in the design doc) */
+    uint32_t *trace;      /* optional: accept bits, ceil(N m / 32) words per step; coloring and
+                             sa_naive set bit k m + y for iteration k of trotter y, naive bit t
+                             for trial t */
     unsigned long long *accepted; /* optional: accepted-flip counter (atomically added) */
     const float *G;       /* nSteps transverse fields (kT for SA), device memory; or NULL: use Gs */
     const float *beta;    /* nSteps inverse temperatures (ignored by SA); or NULL: use betas */
@@ -83,7 +85,8 @@ typedef struct sq103_dense_task {
     int flags;            /* 0 = choose the kernel, 1 = one CTA per instance, 2 = one CTA per trotter */
 } sq103_dense_task;
 
-/* workspace the multi-CTA sweep needs for nSteps steps (accept logs, progress words) */
+/* workspace the multi-CTA sweep needs for nSteps steps (one 64-bit accept word per trotter and
+ * 32 iterations) */
 SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps);
 /* 1 if the one-CTA-per-trotter sweep can run this shape on the current device */
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
@@ -95,7 +98,8 @@ SQ103_API int sq103_dense_hamiltonian(const float *W, int ldW, int N, int maximi
 /* F = q J for all trotters (the local-field refresh). */
 SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q, float *F, int N, int m,
                                         void *stream);
-/* FP64 Ising energies of all trotters (calculate_E; sqaodc/cuda/DeviceFormulas.cpp:42-49).
+/* FP64 Ising energies of all trotters (calculate_E; sqaodc/cuda/DeviceFormulas.cpp:42-49);
+ * the row sums q J are accumulated in double-float (about 2^-44 relative).
  * r_scratch: m x N doubles. */
 SQ103_API int sq103_dense_energy(const float *J, int ldJ, const float *h, const double *c64,
                                  const int8_t *q, int N, int m, int maximize, double *r_scratch,

@@ -9,16 +9,19 @@
 //   c = -1/4 sum(W) - 1/2 (sum b0 + sum b1).
 // Sums are accumulated in FP64 with fixed reduction trees (deterministic).
 //
-// spin_gemm: C[y][n] = sum_k q[y][k] * B(k, n) with q in {-1, +1} (int8).
-// Used for the dense field refresh F = q J (J symmetric), the bipartite
-// half-step fields and the energies.  The products are exact.  fp32 outputs
-// (fields) are the FP64 sum, in k order, of fp32 partial sums over 32-wide k
-// chunks: deterministic and within a few fp32 ulps of the exact sum.  FP64
-// outputs (energies) accumulate every product in FP64.
+// Spin x coupling products C[y][n] = sum_k q[y][k] * B(k, n), q in {-1, +1}
+// (int8), every product exact:
+//   field_gemm (field_gemm.cuh): the dense field refresh F = q J (fp32 partial
+//     sums over 32-wide k chunks, compensated fp32 sum of the chunks) and the
+//     dense energy row sums (double-float accumulation of every product);
+//   spin_gemm (spin_gemm.cuh): the bipartite half-step fields (FP64 sum of fp32
+//     chunk partials) and the bipartite energy row sums (FP64).
+// All are deterministic: the order of every addition is fixed.
 #include <cstdio>
 #include <mutex>
 #include <type_traits>
 
+#include "field_gemm.cuh"
 #include "spin_gemm.cuh"
 #include "sq_common.cuh"
 #include "sq_kernels.h"
@@ -208,7 +211,8 @@ SQ103_API int sq103_bipartite_hamiltonian(const float *b0, const float *b1, cons
 SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q, float *F, int N, int m,
                               void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    launch_spin_gemm<false, float>(q, N, J, ldJ, F, N, m, N, N, s);
+    dim3 grid((N + 63) / 64, (m + 63) / 64);
+    field_gemm_kernel<false, float><<<grid, 256, 0, s>>>(q, N, J, ldJ, F, N, m, N, N);
     return (int)cudaGetLastError();
 }
 
@@ -225,7 +229,8 @@ SQ103_API int sq103_bipartite_fields(const float *J, int N0, int N1, const int8_
 SQ103_API int sq103_dense_energy(const float *J, int ldJ, const float *h, const double *c64, const int8_t *q, int N,
                        int m, int maximize, double *r_scratch, double *E64, float *E32, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    launch_spin_gemm<false, double>(q, N, J, ldJ, r_scratch, N, m, N, N, s);
+    dim3 grid((N + 63) / 64, (m + 63) / 64);
+    field_gemm_kernel<true, double><<<grid, 256, 0, s>>>(q, N, J, ldJ, r_scratch, N, m, N, N);
     dg_energy_finish<<<m, 256, 0, s>>>(q, N, h, r_scratch, c64, maximize ? -1. : 1., E64, E32);
     return (int)cudaGetLastError();
 }
