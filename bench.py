@@ -223,6 +223,217 @@ def cpu_reference(W, steps, seed=0):
     return N * N_TROTTERS * len(idx) / dt, a.workers, dt
 
 
+def _sym_uniform(rng, N):
+    W = rng.uniform(-1.0, 1.0, (N, N)).astype(np.float32)
+    return np.triu(W) + np.triu(W, 1).T
+
+
+def _log_uniform_int(rng, lo, hi):
+    return int(round(float(np.exp(rng.uniform(np.log(lo), np.log(hi))))))
+
+
+def batched_workload(n_inst=1024, seed=1):
+    """1024 uneven dense instances: N log-uniform in [64, 2048], m uniform in
+    {8, 16, 32, 64, 128}; instance i draws its couplings from seed 1000 + i."""
+    rng = np.random.default_rng(seed)
+    return [(_log_uniform_int(rng, 64, 2048), int(rng.choice([8, 16, 32, 64, 128])), 1000 + i)
+            for i in range(n_inst)]
+
+
+def served_stream(rate=200.0, duration=60.0, seed=0):
+    """Poisson arrivals; 70 % dense (N log-uniform in [32, 4096]), 30 % bipartite
+    (N0, N1 log-uniform in [32, 2048]); m in {16, 64, 256}; request i draws its
+    couplings from seed 5000 + i."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > duration:
+            return out
+        dense = rng.random() < 0.7
+        m = int(rng.choice([16, 64, 256]))
+        sizes = ((_log_uniform_int(rng, 32, 4096),) if dense else
+                 (_log_uniform_int(rng, 32, 2048), _log_uniform_int(rng, 32, 2048)))
+        out.append({"t": t, "dense": dense, "sizes": sizes, "m": m, "seed": 5000 + len(out)})
+
+
+_POOL = None
+
+
+def _couplings(req):
+    """The request's couplings: a principal submatrix (dense; symmetric) or a block
+    (bipartite) of one seeded 4096 x 4096 symmetric uniform[-1, 1] pool, at an
+    offset drawn from the request's seed -- deterministic per request, and cheap
+    enough to keep up with the arrival rate."""
+    global _POOL
+    if _POOL is None:
+        _POOL = _sym_uniform(np.random.default_rng(12345), 4096)
+    rng = np.random.default_rng(req["seed"])
+    if req["dense"]:
+        N = req["sizes"][0]
+        o = int(rng.integers(0, 4096 - N + 1))
+        return np.ascontiguousarray(_POOL[o:o + N, o:o + N])
+    N0, N1 = req["sizes"]
+    o0, o1 = int(rng.integers(0, 4096 - N0 + 1)), int(rng.integers(0, 4096 - N1 + 1))
+    return (rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32),
+            np.ascontiguousarray(_POOL[o1:o1 + N1, o0:o0 + N0]))
+
+
+def schedule_1000():
+    tau = np.exp(np.log(0.01 / 5.0) / 1000)
+    return (5.0 * tau ** np.arange(1000)).astype(np.float32)
+
+
+def _solve_plain(sq, req, G):
+    """One request alone on the plain single-instance GPU path; FP64 energies."""
+    d = _couplings(req)
+    m = req["m"]
+    if req["dense"]:
+        a = sq.cuda.dense_graph_annealer(d, sq.minimize, n_trotters=m, algorithm="coloring")
+    else:
+        a = sq.cuda.bipartite_graph_annealer(d[0], d[1], d[2], sq.minimize, n_trotters=m, algorithm="coloring")
+    a.seed(req["seed"])
+    a.prepare()
+    a.randomize_spin()
+    a.anneal(G, BETA)
+    a.make_solution()
+    return a.get_E64()
+
+
+def run_served(args, world):
+    """C5: the served mixed stream against the plain path, each for a wall-time window."""
+    import torch
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    reqs = served_stream()
+    G = schedule_1000()
+    T = args.window
+    srv = AnnealServer(budget_bytes=180 << 30, max_slots=args.slots)
+    srv.set_large_limit(args.large)
+    ticks = 0
+    ids, arrival, finish = {}, {}, {}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        now = time.perf_counter() - t0
+        if now >= T:
+            break
+        while k < len(reqs) and reqs[k]["t"] <= now:
+            r, d = reqs[k], _couplings(reqs[k])
+            if r["dense"]:
+                rid = srv.submit_dense(d, r["m"], G, BETA, sq.minimize, seed=r["seed"])
+            else:
+                rid = srv.submit_bipartite(d[0], d[1], d[2], r["m"], G, BETA, sq.minimize, seed=r["seed"])
+            ids[rid], arrival[rid] = k, r["t"]
+            k += 1
+        nc = srv.tick()
+        ticks += 1
+        if nc:
+            t_now = time.perf_counter() - t0
+            for rid in srv.completed():
+                finish[rid] = t_now
+    served_E = {}
+    for rid in list(finish)[:args.check]:
+        served_E[ids[rid]] = srv.result(rid)[0]
+    lat = sorted(finish[r] - arrival[r] for r in finish)
+    served = {"solves": len(finish), "window_s": T, "solves_per_s": len(finish) / T, "submitted": k,
+              "ticks": ticks, "ms_per_tick": 1000.0 * T / max(ticks, 1),
+              "p50_s": lat[len(lat) // 2] if lat else None,
+              "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None}
+    del srv
+    # the plain path: the same requests, in arrival order, one at a time
+    t0 = time.perf_counter()
+    done, plain_E, lat_p = 0, {}, []
+    while time.perf_counter() - t0 < T and done < len(reqs):
+        E = _solve_plain(sq, reqs[done], G)
+        if done in served_E:
+            plain_E[done] = E
+        lat_p.append(time.perf_counter() - t0 - reqs[done]["t"])
+        done += 1
+    tp = time.perf_counter() - t0
+    lat_p.sort()
+    plain = {"solves": done, "window_s": tp, "solves_per_s": done / tp,
+             "p50_s": lat_p[len(lat_p) // 2] if lat_p else None,
+             "p99_s": lat_p[min(len(lat_p) - 1, int(0.99 * len(lat_p)))] if lat_p else None}
+    rel = [float(np.max(np.abs(served_E[i] - plain_E[i]) / np.maximum(np.abs(plain_E[i]), 1e-30)))
+           for i in plain_E]
+    line = {"metric": "served vs plain solves/s (mixed stream)", "value": served["solves_per_s"],
+            "unit": "solves/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Poisson stream, uniform[-1,1] couplings)",
+            "config": {"workload": ("Poisson 200 req/s, 70 pct dense N log-uniform [32, 4096], 30 pct bipartite "
+                                    "N0/N1 log-uniform [32, 2048], m in {16, 64, 256}, 1000-step G 5.0 -> 0.01, "
+                                    "beta=50; served and plain each for a %.0f s wall-time window") % T,
+                       "slots": args.slots, "large_limit": args.large, "admission_bytes": 180 << 30},
+            "served": served, "plain": plain,
+            "served_over_plain": served["solves_per_s"] / max(plain["solves_per_s"], 1e-30),
+            "energy_check": {"requests": len(rel), "max_rel_diff": max(rel) if rel else None}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batched(args, world):
+    """C4: 1024 uneven instances in one persistent graph-captured launch per
+    annealOneStep, against sequential plain solves of a sample of them."""
+    import torch
+    import sqaod_gb300 as sq
+    from sqaod_gb300.batch import DenseBatchAnnealer
+    work = batched_workload()
+    sched = np.array(schedule(), np.float32)
+    steps = len(sched) if args.batch_steps <= 0 else min(args.batch_steps, len(sched))
+    G = sched[:steps]
+    b = DenseBatchAnnealer()
+    t_add = time.perf_counter()
+    for N, m, seed in work:
+        b.add(_sym_uniform(np.random.default_rng(seed), N), m, sq.minimize, seed)
+    b.set_schedule(G, BETA)
+    b.prepare()
+    smem = b.autotune(2)
+    t_add = time.perf_counter() - t_add
+    b.anneal(1, use_graph=True)  # capture + warm up
+    b.sync()
+    b.prepare()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.anneal(steps, use_graph=True)
+    b.sync()
+    t_batch = time.perf_counter() - t0
+    trials = float(sum(N * m for N, m, _ in work)) * steps
+    # plain path on a sample
+    sample = list(range(0, len(work), len(work) // args.plain_sample))[:args.plain_sample]
+    t_plain, rel = 0.0, []
+    for i in sample:
+        N, m, seed = work[i]
+        W = _sym_uniform(np.random.default_rng(seed), N)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        a = sq.cuda.dense_graph_annealer(W, sq.minimize, n_trotters=m, algorithm="coloring")
+        a.seed(seed)
+        a.prepare()
+        a.randomize_spin()
+        a.anneal(G, BETA)
+        a.make_solution()
+        E = a.get_E64()
+        t_plain += time.perf_counter() - t1
+        Eb = b.get_E64(i)
+        rel.append(float(np.max(np.abs(Eb - E) / np.maximum(np.abs(E), 1e-30))))
+        del a
+    sample_trials = float(sum(work[i][0] * work[i][1] for i in sample)) * steps
+    plain_tps = sample_trials / t_plain
+    line = {"metric": "batched vs plain dense anneals (1024 uneven instances)",
+            "value": trials / t_batch, "unit": "trials/s", "n_gpus": world, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (W uniform[-1,1] symmetric, seed 1000 + i)",
+            "config": {"workload": "1024 dense instances, N log-uniform [64, 2048], m in {8..128}, coloring, "
+                                   "beta=50, %d steps of G=5*0.99^k" % steps, "smem_per_cta": smem},
+            "batched": {"seconds": t_batch, "solves_per_s": len(work) / t_batch, "setup_s": t_add},
+            "plain": {"sample": len(sample), "seconds": t_plain, "trials_per_s": plain_tps,
+                      "solves_per_s_extrapolated": len(work) / (trials / plain_tps),
+                      "note": "sequential single-instance solves of an evenly spaced sample, extrapolated by trials"},
+            "batched_over_plain": (trials / t_batch) / plain_tps,
+            "energy_check": {"instances": len(rel), "max_rel_diff": max(rel) if rel else None}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -253,6 +464,14 @@ def main():
     ap.add_argument("--size", default="%d,%d" % (N_SPINS, N_TROTTERS),
                     help="N,m of the instance (smaller cases are for profiling captures only)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "batched", "served"],
+                    help="sweep: the headline dense sweep; batched: 1024 uneven instances; served: mixed stream")
+    ap.add_argument("--window", type=float, default=20.0, help="served mode: seconds per path")
+    ap.add_argument("--slots", type=int, default=512, help="served mode: concurrent instances per kind")
+    ap.add_argument("--large", type=int, default=4, help="served mode: concurrent whole-GPU instances")
+    ap.add_argument("--check", type=int, default=16, help="served mode: requests compared with the plain path")
+    ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")
+    ap.add_argument("--plain-sample", type=int, default=16, help="batched mode: instances solved on the plain path")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -264,6 +483,10 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.mode != "sweep":
+        if rank == 0:
+            (run_batched if args.mode == "batched" else run_served)(args, world)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

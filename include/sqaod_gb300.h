@@ -88,7 +88,8 @@ typedef struct sq103_dense_task {
 /* workspace the multi-CTA sweep needs for nSteps steps (one 64-bit accept word per trotter and
  * 32 iterations) */
 SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps);
-/* 1 if the one-CTA-per-trotter sweep can run this shape on the current device */
+/* 1 if the one-CTA-per-trotter sweep can run this shape on the current device (N >= 64, m >= 2;
+ * the launch also needs ldJ % 4 == 0 and a 16-byte aligned J) */
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
 
 /* QUBO -> Ising (h, J, c); replaces DeviceDenseGraphFormulas::calculateHamiltonian
@@ -343,10 +344,11 @@ SQ103_API int sq103_dense_batch_get_q(void *handle, int index, int8_t *q, int ca
 
 /* ------------------------------------------- handle layer: request server */
 /* Continuous batching of anneal requests of mixed size and type (no
- * counterpart in the reference).  Requests are admitted FIFO while their
- * device-memory footprint fits budgetBytes and a slot is free; every
- * sq103_server_tick advances every active instance by one annealOneStep and
- * completes the finished ones (FP64 energies, spins).  Each request ends
+ * counterpart in the reference).  Requests are admitted in arrival order while
+ * their device-memory footprint fits budgetBytes and a slot is free (one that
+ * cannot start yet does not block the ones behind it); every
+ * sq103_server_tick advances every active instance by 8 annealOneSteps (one
+ * field-refresh period) and completes the finished ones (FP64 energies, spins).  Each request ends
  * exactly as the same seed and schedule would alone (sq103_dg_annealer /
  * sq103_bg_annealer with prepare, randomize_spin and the schedule; the
  * coloring algorithm for m > 1, sa_naive (dense) or sa_coloring (bipartite)
@@ -367,6 +369,12 @@ SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int
                                   long long capBytes, int release);
 SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *done,
                                  unsigned long long *bytesInUse);
+/* at most n instances on the whole-GPU paths at a time (default 4; dense: one CTA per
+ * trotter, bipartite: per-instance kernels): each
+ * of them steps with the whole GPU every tick */
+SQ103_API int sq103_server_set_large_limit(void *handle, int n);
+/* ids of the requests completed since the last call (at most cap, in completion order) */
+SQ103_API int sq103_server_completed(void *handle, int *ids, int cap, int *n);
 
 #ifdef __cplusplus
 }

@@ -101,6 +101,10 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
 
     const uint32_t wordsPerStep = (uint32_t)(((size_t)N * m + 31) / 32);
     unsigned long long accepted = 0;
+    // flip-list buffer of the next phase; its counter is zero at the start of every
+    // phase (the one of the other buffer is cleared after each phase), so the
+    // alternation continues across steps
+    int buf = 0;
     __shared__ Flip naiveFlip;
     __shared__ int naiveAcc;
 
@@ -140,7 +144,6 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
 
         const bool sa = (T.algo == kSANaive);
         const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
-        int buf = 0;
         for (int k = 0; k < N; ++k) {
             for (int ph = 0; ph < 3; ++ph) {
                 int yb, ys, cnt;
@@ -308,8 +311,9 @@ SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
     if (!task || task->N <= 0 || task->m <= 0 || task->nSteps < 0) return kErrBadShape;
     if (task->nSteps == 0) return 0;
     // one CTA per trotter when the shape allows it (or when asked to), else one CTA
+    const bool rowsAligned = !(task->ldJ & 3) && !(reinterpret_cast<uintptr_t>(task->J) & 15);
     bool multi = task->flags == 2 ||
-                 (task->flags == 0 && task->ws &&
+                 (task->flags == 0 && task->ws && rowsAligned &&
                   task->wsBytes >= sq103_dense_ws_bytes(task->N, task->m, task->nSteps) &&
                   sq103_dense_multicta_ok(task->N, task->m, task->algo));
     if (multi) {

@@ -765,6 +765,16 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_t
                     if (c < n4) F4[c] = f[t];
                 }
             }
+            // the last N % 4 fields (J rows start on 16-byte boundaries: ldJ % 4 == 0)
+            if (ut < N - 4 * n4) {
+                const int i = 4 * n4 + ut;
+                float f = Fs[i];
+                for (int q = 0; q < nf; ++q) {
+                    const int2 fl = flips[q];
+                    f = __fmaf_rn(__int_as_float(fl.y), __ldg(T.J + (size_t)fl.x * T.ldJ + i), f);
+                }
+                Fs[i] = f;
+            }
             __threadfence_block();
             bar_arrive(2, kBarCount);
         }
@@ -821,7 +831,7 @@ SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps) {
 
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo) {
     if (algo != kColoring && algo != kSANaive) return 0;
-    if (N < 64 || (N & 3) || m < 2) return 0;
+    if (N < 64 || m < 2) return 0;
     return m <= multi_capacity(N) ? 1 : 0;
 }
 
@@ -830,6 +840,8 @@ int sq103_dense_anneal_multi(const sq103_dense_task *t, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     const int N = t->N, m = t->m;
     if ((long long)t->nSteps * N >= (1ll << 31)) return kErrBadShape;
+    // rows of J are read as float4
+    if ((t->ldJ & 3) || (reinterpret_cast<uintptr_t>(t->J) & 15)) return kErrBadShape;
     if (!t->ws || t->wsBytes < sq103_dense_ws_bytes(N, m, t->nSteps)) return kErrCapacity;
     if (multi_capacity(N) < m) return kErrCapacity;
     unsigned long long *outLog = reinterpret_cast<unsigned long long *>(t->ws);

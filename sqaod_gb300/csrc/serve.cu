@@ -1,14 +1,17 @@
 // serve.cu -- continuous-batching request server for anneals of mixed size and type.
 //
 // Requests (dense or bipartite QUBO, own N, m, seed and G/beta schedule) are
-// admitted first-in first-out as soon as their device-memory footprint fits
-// the budget and a slot is free.  Admitted instances stay resident (couplings,
+// admitted in arrival order as soon as their device-memory footprint fits the
+// budget and a slot is free (a request that cannot start yet does not block
+// the ones behind it).  Admitted instances stay resident (couplings,
 // spins, fields; the RNG state is (seed, step) and lives in the task).  Every
-// tick advances every active instance by one annealOneStep:
-//   - dense instances whose spins and fields fit in shared memory, and every
-//     bipartite instance, in the persistent batch kernels (one launch each,
+// tick advances every active instance by 8 annealOneSteps (one field-refresh
+// period):
+//   - dense instances whose spins and fields fit in shared memory, and small
+//     bipartite instances, in the persistent batch kernels (one launch each,
 //     instance count read on the device);
-//   - large dense instances with the one-CTA-per-trotter kernel;
+//   - large dense instances with the one-CTA-per-trotter kernel and large
+//     bipartite instances with the per-instance kernels, a few at a time;
 //   - dense fields are refreshed every 8 steps, as the single-instance annealer
 //     does, so each instance ends exactly as it would alone.
 // Finished instances get their FP64 energies and spins copied out, and their
@@ -31,6 +34,10 @@ namespace sq = sqaod;
 class Server : public sq::NullBase {
 public:
     static constexpr int kRefreshPeriod = 8;
+    static constexpr int kStepsPerTick = kRefreshPeriod;  // refreshes fall on tick boundaries
+    // bipartite instances with more spin x coupling products per half step than this
+    // take the per-instance path (GEMMs over the whole GPU) instead of one CTA
+    static constexpr size_t kBipLargeWork = (size_t)1 << 22;
     enum State { kQueued = 0, kActive = 1, kDone = 2 };
 
     struct Request {
@@ -102,32 +109,43 @@ public:
         return enqueue(std::move(rq), m, optimize, seed, G, beta, nSteps);
     }
 
-    // one step of every active instance; returns the number of requests completed
+    // kStepsPerTick steps (one refresh period) of every active instance; returns the
+    // number of requests completed
     int tick() {
         admit();
         const int nD = (int)denseSlots_.size(), nB = (int)bipSlots_.size();
         if (nD > 0)
-            SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, nD, counts_.p, nullptr, dPos_.p, queues_.p, 1,
+            SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, nD, counts_.p, nullptr, dPos_.p, queues_.p, kStepsPerTick,
                                               std::min(denseGrid_, nD), stageSmem_, st_.get()));
         if (nB > 0)
-            SQ_CHECK(sq103_bipartite_batch_launch(bTasks_.p, nB, counts_.p + 1, nullptr, bPos_.p, queues_.p + 2, 1,
-                                                  std::min(bipGrid_, nB), st_.get()));
+            SQ_CHECK(sq103_bipartite_batch_launch(bTasks_.p, nB, counts_.p + 1, nullptr, bPos_.p, queues_.p + 2,
+                                                  kStepsPerTick, std::min(bipGrid_, nB), st_.get()));
         for (Request *r : large_) {
-            sq103_dense_task t = r->dt;
-            t.G = r->dt.G + r->pos;
-            t.beta = r->dt.beta + r->pos;
-            t.step0 = 1 + (uint32_t)r->pos;
-            t.nSteps = 1;
-            t.ws = ws_.p;
-            t.wsBytes = ws_.n;
-            SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
+            const int n = std::min(kStepsPerTick, r->nSteps - r->pos);
+            if (r->kind == 0) {
+                sq103_dense_task t = r->dt;
+                t.G = r->dt.G + r->pos;
+                t.beta = r->dt.beta + r->pos;
+                t.step0 = 1 + (uint32_t)r->pos;
+                t.nSteps = n;
+                t.ws = ws_.p;
+                t.wsBytes = ws_.n;
+                SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
+            } else {
+                sq103_bipartite_task t = r->bt;
+                t.G = r->bt.G + r->pos;
+                t.beta = r->bt.beta + r->pos;
+                t.step0 = 1 + (uint32_t)r->pos;
+                t.nSteps = n;
+                SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
+            }
         }
         std::vector<Request *> finished;
         for (auto &kv : active_) {
             Request *r = kv.second;
-            r->pos += 1;
+            r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)
-                SQ_CHECK(sq103_dense_field_refresh(r->dt.J, r->N0, r->dt.q, r->dt.F, r->N0, r->m, st_.get()));
+                SQ_CHECK(sq103_dense_field_refresh(r->dt.J, r->dt.ldJ, r->dt.q, r->dt.F, r->N0, r->m, st_.get()));
             if (r->pos >= r->nSteps) finished.push_back(r);
         }
         for (Request *r : finished) complete(r);
@@ -152,6 +170,19 @@ public:
         throwErrorIf(it == all_.end(), "unknown request id %d.", id);
         throwErrorIf(it->second->state != kDone, "request %d is not done.", id);
         all_.erase(it);
+    }
+
+    // ids completed since the last call, in completion order
+    int drainCompleted(int *ids, int cap) {
+        const int n = std::min<int>(cap, (int)completed_.size());
+        for (int i = 0; i < n; ++i) ids[i] = completed_[i];
+        completed_.erase(completed_.begin(), completed_.begin() + n);
+        return n;
+    }
+
+    void setLargeLimit(int n) {
+        throwErrorIf(n < 1, "the large-instance limit must be at least 1.");
+        maxLarge_ = n;
     }
 
     void stats(int *queued, int *active, int *done, unsigned long long *bytes) const {
@@ -181,12 +212,13 @@ private:
     }
 
     static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+    static size_t ldj(size_t N) { return (N + 3) & ~(size_t)3; }
 
     static size_t footprint(const Request &r) {
         size_t s = 8 * 256 + al(r.nSteps * 4) * 2;
         if (r.kind == 0) {
             size_t N = r.N0, m = r.m;
-            s += al(N * N * 4) + al(N * 4) + al(m * N * 4) + al(m * N) + al(m * N * 8);
+            s += al(N * ldj(N) * 4) + al(N * 4) + al(m * N * 4) + al(m * N) + al(m * N * 8);
         } else {
             size_t N0 = r.N0, N1 = r.N1, m = r.m;
             s += al(N0 * N1 * 4) + al(N0 * 4) + al(N1 * 4) + al(m * N0) + al(m * N1) + al(m * N0 * 4) +
@@ -200,14 +232,25 @@ private:
         return base + (size_t)r.m * r.N0 * 5 + (size_t)r.N0 * 4 <= (size_t)stageSmem_;
     }
 
+    // Admits queued requests in arrival order as memory, slots and the large-instance
+    // limit allow; a request that cannot start yet keeps its place and does not
+    // block the ones behind it.
     void admit() {
         bool changed = false;
-        while (!queue_.empty()) {
-            Request *r = queue_.front();
-            if (used_ + r->bytes > budget_) break;
-            bool large = r->kind == 0 && !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring);
-            if (!large && (int)(r->kind == 0 ? denseSlots_.size() : bipSlots_.size()) >= maxSlots_) break;
-            queue_.pop_front();
+        size_t i = 0;
+        while (i < queue_.size()) {
+            Request *r = queue_[i];
+            const bool large = r->kind == 0 ? !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring)
+                                            : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork;
+            const bool fits =
+                used_ + r->bytes <= budget_ &&
+                (large ? (int)large_.size() < maxLarge_  // each steps with the whole GPU every tick
+                       : (int)(r->kind == 0 ? denseSlots_.size() : bipSlots_.size()) < maxSlots_);
+            if (!fits) {
+                ++i;
+                continue;
+            }
+            queue_.erase(queue_.begin() + i);
             r->large = large;
             setup(r);
             used_ += r->bytes;
@@ -217,8 +260,8 @@ private:
         }
         if (changed) {
             int c[2] = {(int)denseSlots_.size(), (int)bipSlots_.size()};
+            // (pageable source: staged before the call returns)
             SQ_CHECK(cudaMemcpyAsync(counts_.p, c, sizeof(c), cudaMemcpyHostToDevice, st_.get()));
-            st_.sync();  // the host array above is a temporary
         }
     }
 
@@ -226,7 +269,8 @@ private:
         const int m = r->m, n = r->nSteps;
         if (r->kind == 0) {
             const size_t N = r->N0;
-            size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * N * 4), oc = oh + al(N * 4),
+            const size_t ldJ = ldj(N);  // rows padded to 16 bytes for the one-CTA-per-trotter sweep
+            size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * ldJ * 4), oc = oh + al(N * 4),
                    oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), tot = oR + al(m * N * 8);
             r->mem.ensure(tot);
             unsigned char *b = r->mem.p;
@@ -240,19 +284,20 @@ private:
             SQ_CHECK(cudaMemcpyAsync(beta, r->beta.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
             dW_.ensure(N * N);
             SQ_CHECK(cudaMemcpyAsync(dW_.p, r->W.data(), 4 * N * N, cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(sq103_dense_hamiltonian(dW_.p, (int)N, (int)N, r->optimize, h, J, (int)N, c32, r->c64, scratch,
+            SQ_CHECK(cudaMemsetAsync(J, 0, sizeof(float) * N * ldJ, st_.get()));
+            SQ_CHECK(sq103_dense_hamiltonian(dW_.p, (int)N, (int)N, r->optimize, h, J, (int)ldJ, c32, r->c64, scratch,
                                              st_.get()));
             SQ_CHECK(sq103_randomize_spins(q, (int)N, m, r->seed, 0, 0, st_.get()));
-            SQ_CHECK(sq103_dense_field_refresh(J, (int)N, q, F, (int)N, m, st_.get()));
+            SQ_CHECK(sq103_dense_field_refresh(J, (int)ldJ, q, F, (int)N, m, st_.get()));
             sq103_dense_task &t = r->dt;
             t = sq103_dense_task{};
             t.J = J; t.h = h; t.q = q; t.F = F; t.G = G; t.beta = beta;
-            t.seed = r->seed; t.step0 = 1; t.N = (int)N; t.m = m; t.ldJ = (int)N;
+            t.seed = r->seed; t.step0 = 1; t.N = (int)N; t.m = m; t.ldJ = (int)ldJ;
             t.algo = m == 1 ? kSANaive : kColoring;
             t.nSteps = n;
             t.status = status_.p;
             if (r->large) {
-                ws_.ensure(std::max<unsigned long long>(ws_.n, sq103_dense_ws_bytes((int)N, m, 1)));
+                ws_.ensure(std::max<unsigned long long>(ws_.n, sq103_dense_ws_bytes((int)N, m, kStepsPerTick)));
                 large_.push_back(r);
             } else {
                 r->slot = (int)denseSlots_.size();
@@ -291,13 +336,18 @@ private:
             t.N0 = (int)N0; t.N1 = (int)N1; t.m = m;
             t.algo = m == 1 ? kSAColoring : kColoring;
             t.nSteps = n;
-            r->slot = (int)bipSlots_.size();
-            bipSlots_.push_back(r);
-            int zero = 0;
-            SQ_CHECK(cudaMemcpyAsync(bTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(bPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+            if (r->large) {
+                large_.push_back(r);
+            } else {
+                r->slot = (int)bipSlots_.size();
+                bipSlots_.push_back(r);
+                int zero = 0;
+                SQ_CHECK(cudaMemcpyAsync(bTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
+                SQ_CHECK(cudaMemcpyAsync(bPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+            }
         }
-        st_.sync();  // r->W and the task structs above are read before this returns
+        // copies from pageable host memory return once the data is staged, so
+        // r->W and the task structs above may go now
         r->W.clear();
         r->W.shrink_to_fit();
     }
@@ -311,7 +361,8 @@ private:
         if (r->kind == 0) {
             const int N = r->N0;
             double *scratch = (double *)((unsigned char *)r->dt.q + al((size_t)m * N));
-            SQ_CHECK(sq103_dense_energy(r->dt.J, N, r->dt.h, r->c64, r->dt.q, N, m, r->optimize, scratch, E.p, nullptr,
+            SQ_CHECK(sq103_dense_energy(r->dt.J, r->dt.ldJ, r->dt.h, r->c64, r->dt.q, N, m, r->optimize, scratch, E.p,
+                                        nullptr,
                                         st_.get()));
             r->q0.resize((size_t)m * N);
             SQ_CHECK(cudaMemcpyAsync(r->q0.data(), r->dt.q, (size_t)m * N, cudaMemcpyDeviceToHost, st_.get()));
@@ -332,13 +383,14 @@ private:
         throwErrorIf(status != 0, "a dense sweep kernel reported status %d.", status);
         // free the slot: the last slot moves into it
         if (r->kind == 0 && !r->large) removeSlot(denseSlots_, r, dTasks_.p, dPos_.p, 0);
-        if (r->kind == 1) removeSlot(bipSlots_, r, bTasks_.p, bPos_.p, 1);
+        if (r->kind == 1 && !r->large) removeSlot(bipSlots_, r, bTasks_.p, bPos_.p, 1);
         if (r->large) large_.erase(std::find(large_.begin(), large_.end(), r));
         st_.sync();
         r->mem.release();
         used_ -= r->bytes;
         active_.erase(r->id);
         r->state = kDone;
+        completed_.push_back(r->id);
         ++done_;
     }
 
@@ -361,11 +413,12 @@ private:
 
     Stream st_;
     unsigned long long budget_, used_ = 0;
-    int maxSlots_, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
+    int maxSlots_, maxLarge_ = 4, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
     long long ticks_ = 0;
     int hostCount_[2] = {0, 0};
     std::map<int, std::unique_ptr<Request>> all_;
     std::deque<Request *> queue_;
+    std::deque<int> completed_;
     std::map<int, Request *> active_;
     std::vector<Request *> denseSlots_, bipSlots_, large_;
     DevBuf<sq103_dense_task> dTasks_;
@@ -448,6 +501,16 @@ SQ103_API int sq103_server_result(void *h, int id, double *E, int capE, int *m, 
         if (q0) memcpy(q0, r.q0.data(), r.q0.size());
         if (q1 && !r.q1.empty()) memcpy(q1, r.q1.data(), r.q1.size());
         if (release) s->release(id);
+    });
+}
+SQ103_API int sq103_server_set_large_limit(void *h, int n) {
+    return serve_guard([&] { as_server(h)->setLargeLimit(n); });
+}
+SQ103_API int sq103_server_completed(void *h, int *ids, int cap, int *n) {
+    return serve_guard([&] {
+        throwErrorIf(ids == nullptr && cap > 0, "null argument");
+        const int k = as_server(h)->drainCompleted(ids, cap);
+        if (n) *n = k;
     });
 }
 SQ103_API int sq103_server_stats(void *h, int *queued, int *active, int *done, unsigned long long *bytesInUse) {

@@ -99,9 +99,9 @@ public:
         allocProblem();
         DevBuf<float> dW;
         dW.ensure((size_t)N_ * N_);
-        upload(dW.p, W);
-        SQ_CHECK(sq103_dense_hamiltonian(dW.p, N_, N_, om == sq::optMaximize, d_h_.p, d_J_.p, N_, d_c_.p, d_c64_.p,
-                                         d_scratchN_.p, st_.get()));
+        upload(dW.p, N_, W);
+        SQ_CHECK(sq103_dense_hamiltonian(dW.p, N_, N_, om == sq::optMaximize, d_h_.p, d_J_.p, ldJ_, d_c_.p,
+                                         d_c64_.p, d_scratchN_.p, st_.get()));
         st_.sync();
         setState(solProblemSet);
     }
@@ -116,7 +116,7 @@ public:
         om_ = sq::optMinimize;
         allocProblem();
         SQ_CHECK(cudaMemcpyAsync(d_h_.p, h.data, sizeof(float) * N_, cudaMemcpyHostToDevice, st_.get()));
-        upload(d_J_.p, J);
+        upload(d_J_.p, ldJ_, J);
         double c64 = (double)c;
         SQ_CHECK(cudaMemcpyAsync(d_c_.p, &c, sizeof(float), cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c64, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
@@ -129,8 +129,8 @@ public:
         h->resize(N_);
         J->resize(N_, N_);
         SQ_CHECK(cudaMemcpyAsync(h->data, d_h_.p, sizeof(float) * N_, cudaMemcpyDeviceToHost, st_.get()));
-        SQ_CHECK(cudaMemcpy2DAsync(J->data, sizeof(float) * J->stride, d_J_.p, sizeof(float) * N_, sizeof(float) * N_,
-                                   N_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpy2DAsync(J->data, sizeof(float) * J->stride, d_J_.p, sizeof(float) * ldJ_,
+                                   sizeof(float) * N_, N_, cudaMemcpyDeviceToHost, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(c, d_c_.p, sizeof(float), cudaMemcpyDeviceToHost, st_.get()));
         const_cast<Stream &>(st_).sync();
     }
@@ -197,7 +197,7 @@ public:
         throwErrorIfQNotSet();
         checkStatus();
         d_r_.ensure((size_t)m_ * N_);
-        SQ_CHECK(sq103_dense_energy(d_J_.p, N_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize, d_r_.p,
+        SQ_CHECK(sq103_dense_energy(d_J_.p, ldJ_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize, d_r_.p,
                                     d_E64_.p, d_E32_.p, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(h_E64_.p, d_E64_.p, sizeof(double) * m_, cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
@@ -276,15 +276,18 @@ public:
 
 private:
     void allocProblem() {
-        d_J_.ensure((size_t)N_ * N_);
+        // rows of J padded to 16 bytes (the one-CTA-per-trotter sweep reads them as float4)
+        ldJ_ = (N_ + 3) & ~3;
+        d_J_.ensure((size_t)N_ * ldJ_);
+        SQ_CHECK(cudaMemsetAsync(d_J_.p, 0, sizeof(float) * N_ * ldJ_, st_.get()));
         d_h_.ensure(N_);
         d_c_.ensure(1);
         d_c64_.ensure(1);
         d_scratchN_.ensure(N_);
     }
 
-    void upload(float *dst, const Matrix &M) {
-        SQ_CHECK(cudaMemcpy2DAsync(dst, sizeof(float) * M.cols, M.data, sizeof(float) * M.stride,
+    void upload(float *dst, int ldDst, const Matrix &M) {
+        SQ_CHECK(cudaMemcpy2DAsync(dst, sizeof(float) * ldDst, M.data, sizeof(float) * M.stride,
                                    sizeof(float) * M.cols, M.rows, cudaMemcpyHostToDevice, st_.get()));
         st_.sync();  // M may be a temporary of the caller
     }
@@ -297,7 +300,7 @@ private:
     }
 
     void refreshFields() {
-        SQ_CHECK(sq103_dense_field_refresh(d_J_.p, N_, d_q_.p, d_F_.p, N_, m_, st_.get()));
+        SQ_CHECK(sq103_dense_field_refresh(d_J_.p, ldJ_, d_q_.p, d_F_.p, N_, m_, st_.get()));
         stepsSinceRefresh_ = 0;
     }
 
@@ -339,7 +342,7 @@ private:
             t.step0 = step_;
             t.N = N_;
             t.m = m_;
-            t.ldJ = N_;
+            t.ldJ = ldJ_;
             t.algo = algo;
             t.nSteps = chunk;
             t.status = d_status_.p;
@@ -388,6 +391,7 @@ private:
 
     mutable Stream st_;
     DevBuf<float> d_J_, d_h_, d_c_, d_F_, d_E32_, d_sched_;
+    int ldJ_ = 0;  // row stride of J
     DevBuf<double> d_c64_, d_scratchN_, d_E64_, d_r_;
     DevBuf<int8_t> d_q_;
     DevBuf<unsigned long long> d_acc_;

@@ -1,9 +1,10 @@
 """Request server: continuous batching of anneal requests of mixed size and type.
 
 Requests (dense or bipartite QUBOs, each with its own trotter count, seed and
-G/beta schedule) are admitted first-in first-out while their device-memory
-footprint fits the budget.  Every tick() advances every admitted request by
-one annealOneStep; finished requests get their FP64 energies and spins
+G/beta schedule) are admitted in arrival order while their device-memory
+footprint fits the budget and a slot is free; one that cannot start yet does
+not block the ones behind it.  Every tick() advances every admitted request by
+8 annealOneSteps (one field-refresh period); finished requests get their FP64 energies and spins
 copied out and free their memory in the same tick.
 
 A request with m > 1 trotters runs SQA with the coloring sweep; m == 1 runs
@@ -77,7 +78,7 @@ class AnnealServer:
         return rid.value
 
     def tick(self):
-        """One annealOneStep of every active request; returns how many finished."""
+        """8 annealOneSteps of every active request; returns how many finished."""
         c = ctypes.c_int()
         self._call("tick", ctypes.byref(c))
         return c.value
@@ -92,6 +93,17 @@ class AnnealServer:
         b = ctypes.c_ulonglong()
         self._call("stats", *[ctypes.byref(x) for x in v], ctypes.byref(b))
         return {"queued": v[0].value, "active": v[1].value, "done": v[2].value, "bytes_in_use": b.value}
+
+    def set_large_limit(self, n):
+        """At most n dense instances on the one-CTA-per-trotter path at a time."""
+        self._call("set_large_limit", ctypes.c_int(int(n)))
+
+    def completed(self, cap=4096):
+        """Ids of the requests completed since the last call, in completion order."""
+        ids = np.zeros(cap, np.int32)
+        n = ctypes.c_int()
+        self._call("completed", ptr(ids), ctypes.c_int(cap), ctypes.byref(n))
+        return ids[:n.value].tolist()
 
     def result(self, rid, release=True):
         """(E, q) of a finished request: m FP64 energies and the spins, q of

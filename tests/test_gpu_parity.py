@@ -197,7 +197,7 @@ def test_bipartite_sweep_replays_fp64(sq, orc, algo, N0, N1, m):
 
 
 @pytest.mark.parametrize("algo", ["coloring", "sa_naive"])
-@pytest.mark.parametrize("N,m", [(128, 16), (256, 7), (96, 2), (512, 64)])
+@pytest.mark.parametrize("N,m", [(128, 16), (256, 7), (96, 2), (512, 64), (130, 16), (1023, 37)])
 def test_dense_multi_cta_equals_single_cta(sq, algo, N, m):
     """One CTA per trotter (cooperative) and one CTA per instance run the same
     trials with the same fp32 arithmetic: spins and FP64 energies bit-identical."""
@@ -238,6 +238,32 @@ def test_dense_multi_cta_equals_single_cta_large(sq, N, m):
     assert out[0][2] == out[1][2]
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("flags", [1, 2])
+@pytest.mark.parametrize("algo,N,m", [("sa_naive", 1023, 8), ("coloring", 1023, 37), ("coloring", 97, 5)])
+def test_dense_multi_step_launch_replays_fp64(sq, orc, flags, algo, N, m):
+    """Several steps in one launch (anneal over a schedule), odd N and odd
+    phase counts per step, both kernels: every step replays against FP64."""
+    rng = np.random.default_rng(N + m)
+    W = rand_sym(rng, N)
+    G = np.array([5.0 * 0.9 ** k for k in range(3)], np.float32)
+    a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm=algo)
+    a.set_kernel(flags)
+    a.seed(21)
+    a.prepare()
+    a.randomize_spin()
+    q = np.array(a.get_q())
+    h, J, c = a.get_hamiltonian()
+    a.set_trace(True)
+    _, step0 = a.get_rng_state()
+    a.anneal(G, 20.0)
+    nw = (N * m + 31) // 32
+    trace = np.array(a.get_trace(nw * len(G)), np.uint32).reshape(len(G), nw)
+    for s in range(len(G)):
+        q, st = orc.dg_replay(h, J, m, DENSE_ALGOS[algo], 21, step0 + s, float(G[s]), 20.0, q, trace[s], MARGIN_TOL)
+        assert st["n_mismatch"] == st["n_mismatch_small"], (s, st)
+    assert np.array_equal(np.array(a.get_q()), q)
 
 
 @pytest.mark.parametrize("algo", ["coloring", "sa_naive"])

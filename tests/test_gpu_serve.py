@@ -29,6 +29,8 @@ SPECS = [
     ("d", 130, 2, 25, "min"),
     ("b", (48, 48), 8, 11, "max"),
     ("d", 64, 32, 3, "min"),
+    ("d", 1023, 16, 9, "min"),  # one CTA per trotter, row stride padded to 1024
+    ("b", (1024, 512), 16, 7, "min"),  # per-instance bipartite kernels
 ]
 
 
@@ -61,8 +63,10 @@ def test_server_requests_match_alone():
             N0, N1 = sizes
             data.append((rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32),
                          rng.uniform(-1, 1, (N1, N0)).astype(np.float32)))
-    # the N=1024 request (about 5 MB) waits until enough of the others finish
+    # the N=1024 request (about 5 MB) waits until enough of the others finish; one
+    # large instance at a time
     srv = AnnealServer(budget_bytes=6 << 20, max_slots=3)
+    srv.set_large_limit(1)
     ids = []
     for i, (spec, d) in enumerate(zip(SPECS, data)):
         kind, sizes, m, steps, opt = spec
@@ -77,8 +81,8 @@ def test_server_requests_match_alone():
     st = srv.stats()
     assert st["queued"] == 0 and st["active"] == 0 and st["done"] == len(SPECS)
     assert st["bytes_in_use"] == 0
-    # queueing made the run longer than the longest request
-    assert ticks > max(s[3] for s in SPECS)
+    # queueing made the run longer than the longest request (8 steps per tick)
+    assert ticks > -(-max(s[3] for s in SPECS) // 8)
     for i, (spec, d, rid) in enumerate(zip(SPECS, data, ids)):
         assert srv.state(rid) == DONE
         E, q = srv.result(rid)
