@@ -26,13 +26,23 @@ void createBitSetSequence(V *bits, SizeType stride, SizeType nBits, PackedBitSet
 
 void unpackBitSet(BitSet *unpacked, PackedBitSet packed, int N);
 
+// exact W == W^T of an n x n row-major matrix with row stride ld, compared in
+// 64 x 64 tiles so that the transposed reads stay in cache
+template <class real>
+bool isSymmetric(const real *W, size_t n, size_t ld) {
+    const size_t B = 64;
+    for (size_t r0 = 0; r0 < n; r0 += B)
+        for (size_t c0 = 0; c0 <= r0; c0 += B)
+            for (size_t r = r0; r < r0 + B && r < n; ++r)
+                for (size_t c = c0; c < c0 + B && c < r; ++c)
+                    if (W[r * ld + c] != W[c * ld + r]) return false;
+    return true;
+}
+
 template <class real>
 bool isSymmetric(const MatrixType<real> &W) {
     if (W.rows != W.cols) return false;
-    for (SizeType r = 0; r < W.rows; ++r)
-        for (SizeType c = 0; c < r; ++c)
-            if (W(r, c) != W(c, r)) return false;
-    return true;
+    return isSymmetric(W.data, (size_t)W.rows, (size_t)W.stride);
 }
 
 // x = (q + 1) / 2

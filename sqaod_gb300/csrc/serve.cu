@@ -85,9 +85,7 @@ public:
         throwErrorIf(N <= 0 || m <= 0 || nSteps <= 0, "bad request shape.");
         throwErrorIf(sq103_dense_batch_min_smem(m) > stageSmem_ && !sq103_dense_multicta_ok(N, m, kColoring),
                      "%d trotters of %d spins fit neither kernel.", m, N);
-        for (int r = 0; r < N; ++r)
-            for (int c = 0; c < r; ++c)
-                throwErrorIf(W[(size_t)r * N + c] != W[(size_t)c * N + r], "%s, Matrix is not symmetric.", __func__);
+        throwErrorIf(!sqaod::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
         auto rq = std::make_unique<Request>();
         rq->kind = 0;
         rq->N0 = N;

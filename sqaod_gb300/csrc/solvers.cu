@@ -1130,9 +1130,7 @@ public:
     int add(const float *W, int N, int m, int optimize, unsigned long long seed) {
         throwErrorIf(prepared_, "instances must be added before prepare().");
         throwErrorIf(N <= 0 || m <= 0, "N and m must be positive.");
-        for (int r = 0; r < N; ++r)
-            for (int c = 0; c < r; ++c)
-                throwErrorIf(W[(size_t)r * N + c] != W[(size_t)c * N + r], "%s, Matrix is not symmetric.", __func__);
+        throwErrorIf(!sqaod::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
         insts_.emplace_back(new Inst());
         Inst &in = *insts_.back();
         in.N = N;

@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 
 from .. import common
-from .._lib import call, lib, ptr
+from .._lib import SqaodError, call, lib, ptr
 
 _c_int = ctypes.c_int
 _c_float = ctypes.c_float
@@ -104,8 +104,15 @@ class DenseGraphAnnealer(_Handle):
     def set_qubo(self, W, optimize=common.minimize):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
-        W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
-        self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        try:
+            # an exactly symmetric W passes the native check as is
+            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        except SqaodError as e:
+            if 'not symmetric' not in str(e):
+                raise
+            # otherwise the reference's rule: symmetrize a triangular W, reject the rest
+            W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
+            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
         self._optimize = optimize
 
     def set_hamiltonian(self, h, J, c):
@@ -367,8 +374,15 @@ class DenseGraphBFSearcher(_Handle):
     def set_qubo(self, W, optimize=common.minimize):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
-        W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
-        self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        try:
+            # an exactly symmetric W passes the native check as is
+            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        except SqaodError as e:
+            if 'not symmetric' not in str(e):
+                raise
+            # otherwise the reference's rule: symmetrize a triangular W, reject the rest
+            W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
+            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
         self._optimize = optimize
 
     def get_problem_size(self):
