@@ -381,29 +381,38 @@ def run_batched(args, world):
     sched = np.array(schedule(), np.float32)
     steps = len(sched) if args.batch_steps <= 0 else min(args.batch_steps, len(sched))
     G = sched[:steps]
+    Ws = [_sym_uniform(np.random.default_rng(seed), N) for N, m, seed in work]
     b = DenseBatchAnnealer()
     t_add = time.perf_counter()
-    for N, m, seed in work:
-        b.add(_sym_uniform(np.random.default_rng(seed), N), m, sq.minimize, seed)
+    for (N, m, seed), W in zip(work, Ws):
+        b.add(W, m, sq.minimize, seed)
     b.set_schedule(G, BETA)
     b.prepare()
-    smem = b.autotune(2)
+    torch.cuda.synchronize()
     t_add = time.perf_counter() - t_add
+    t_tune = time.perf_counter()
+    smem = b.autotune(2)
     b.anneal(1, use_graph=True)  # capture + warm up
     b.sync()
+    t_tune = time.perf_counter() - t_tune
     b.prepare()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b.anneal(steps, use_graph=True)
     b.sync()
     t_batch = time.perf_counter() - t0
+    t_out = time.perf_counter()
+    for i in range(len(work)):
+        b.get_E64(i)
+    t_out = time.perf_counter() - t_out
     trials = float(sum(N * m for N, m, _ in work)) * steps
+    t_total = t_add + t_batch + t_out
     # plain path on a sample
     sample = list(range(0, len(work), len(work) // args.plain_sample))[:args.plain_sample]
     t_plain, rel = 0.0, []
     for i in sample:
         N, m, seed = work[i]
-        W = _sym_uniform(np.random.default_rng(seed), N)
+        W = Ws[i]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         a = sq.cuda.dense_graph_annealer(W, sq.minimize, n_trotters=m, algorithm="coloring")
@@ -425,11 +434,17 @@ def run_batched(args, world):
             "data": "synthetic (W uniform[-1,1] symmetric, seed 1000 + i)",
             "config": {"workload": "1024 dense instances, N log-uniform [64, 2048], m in {8..128}, coloring, "
                                    "beta=50, %d steps of G=5*0.99^k" % steps, "smem_per_cta": smem},
-            "batched": {"seconds": t_batch, "solves_per_s": len(work) / t_batch, "setup_s": t_add},
+            "batched": {"seconds": t_batch, "solves_per_s": len(work) / t_batch, "setup_s": t_add,
+                        "results_s": t_out, "seconds_with_setup": t_total,
+                        "solves_per_s_with_setup": len(work) / t_total, "autotune_s": t_tune,
+                        "note": "seconds = the annealing launches alone; with_setup adds add()+prepare() of "
+                                "all instances and reading every instance's energies (autotune, a one-off, not)"},
             "plain": {"sample": len(sample), "seconds": t_plain, "trials_per_s": plain_tps,
                       "solves_per_s_extrapolated": len(work) / (trials / plain_tps),
-                      "note": "sequential single-instance solves of an evenly spaced sample, extrapolated by trials"},
+                      "note": "sequential single-instance solves of an evenly spaced sample (set_qubo, prepare, "
+                              "anneal, make_solution, energies), extrapolated by trials"},
             "batched_over_plain": (trials / t_batch) / plain_tps,
+            "batched_over_plain_with_setup": (trials / t_total) / plain_tps,
             "energy_check": {"instances": len(rel), "max_rel_diff": max(rel) if rel else None}}
     print(json.dumps(line), flush=True)
 

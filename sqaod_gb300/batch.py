@@ -39,10 +39,11 @@ class DenseBatchAnnealer:
     def add(self, W, n_trotters, optimize=common.minimize, seed=0):
         """Adds one QUBO instance; returns its index."""
         common.check_square(W)
-        W = np.ascontiguousarray(common.symmetrize(common.fix_type(W, np.float32)), np.float32)
+        W = common.fix_type(W, np.float32)
         idx = ctypes.c_int()
-        self._call("add", ptr(W), ctypes.c_int(W.shape[0]), ctypes.c_int(int(n_trotters)),
-                   ctypes.c_int(common.optimize_flag(optimize)), ctypes.c_ulonglong(int(seed)), ctypes.byref(idx))
+        common.submit_symmetric(W, np.float32, lambda w: self._call(
+            "add", ptr(w), ctypes.c_int(w.shape[0]), ctypes.c_int(int(n_trotters)),
+            ctypes.c_int(common.optimize_flag(optimize)), ctypes.c_ulonglong(int(seed)), ctypes.byref(idx)))
         self._m.append(int(n_trotters))
         self._N.append(W.shape[0])
         return idx.value

@@ -101,6 +101,20 @@ def symmetrize(mat):
     raise RuntimeError("given matrix is not triangular nor symmetric.")
 
 
+def submit_symmetric(W, dtype, submit):
+    """submit(W) with W as given, the native side checking exact symmetry (cheap,
+    cache-tiled); if it rejects W as not symmetric, the reference's rule is
+    applied (a triangular W becomes (W + W^T) / 2, anything else raises) and
+    submit is called again.  Same outcome as symmetrize() first, without its
+    allclose pass over an already symmetric W."""
+    try:
+        return submit(W)
+    except RuntimeError as e:
+        if 'not symmetric' not in str(e):
+            raise
+    return submit(np.ascontiguousarray(symmetrize(W), dtype))
+
+
 def fix_type(obj, dtype):
     if isinstance(obj, np.ndarray):
         if obj.dtype == dtype and obj.flags['C_CONTIGUOUS']:

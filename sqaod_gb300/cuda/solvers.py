@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 
 from .. import common
-from .._lib import SqaodError, call, lib, ptr
+from .._lib import call, lib, ptr
 
 _c_int = ctypes.c_int
 _c_float = ctypes.c_float
@@ -104,15 +104,8 @@ class DenseGraphAnnealer(_Handle):
     def set_qubo(self, W, optimize=common.minimize):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
-        try:
-            # an exactly symmetric W passes the native check as is
-            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
-        except SqaodError as e:
-            if 'not symmetric' not in str(e):
-                raise
-            # otherwise the reference's rule: symmetrize a triangular W, reject the rest
-            W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
-            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        om = _c_int(common.optimize_flag(optimize))
+        common.submit_symmetric(W, self.dtype, lambda w: self._call('set_qubo', ptr(w), _c_int(w.shape[0]), om))
         self._optimize = optimize
 
     def set_hamiltonian(self, h, J, c):
@@ -374,15 +367,8 @@ class DenseGraphBFSearcher(_Handle):
     def set_qubo(self, W, optimize=common.minimize):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
-        try:
-            # an exactly symmetric W passes the native check as is
-            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
-        except SqaodError as e:
-            if 'not symmetric' not in str(e):
-                raise
-            # otherwise the reference's rule: symmetrize a triangular W, reject the rest
-            W = np.ascontiguousarray(common.symmetrize(W), self.dtype)
-            self._call('set_qubo', ptr(W), _c_int(W.shape[0]), _c_int(common.optimize_flag(optimize)))
+        om = _c_int(common.optimize_flag(optimize))
+        common.submit_symmetric(W, self.dtype, lambda w: self._call('set_qubo', ptr(w), _c_int(w.shape[0]), om))
         self._optimize = optimize
 
     def get_problem_size(self):

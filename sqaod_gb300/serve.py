@@ -51,14 +51,16 @@ class AnnealServer:
         return G, beta
 
     def submit_dense(self, W, n_trotters, G, beta, optimize=common.minimize, seed=0):
-        """Queues a dense QUBO anneal; returns its request id."""
+        """Queues a dense QUBO anneal (W symmetric, or triangular as in
+        set_qubo); returns its request id."""
         common.check_square(W)
-        W = np.ascontiguousarray(common.fix_type(W, np.float32), np.float32)
+        W = common.fix_type(W, np.float32)
         G, beta = self._schedule(G, beta)
         rid = ctypes.c_int()
-        self._call("submit_dense", ptr(W), ctypes.c_int(W.shape[0]), ctypes.c_int(int(n_trotters)),
-                   ctypes.c_int(common.optimize_flag(optimize)), ctypes.c_ulonglong(int(seed)), ptr(G), ptr(beta),
-                   ctypes.c_int(len(G)), ctypes.byref(rid))
+        common.submit_symmetric(W, np.float32, lambda w: self._call(
+            "submit_dense", ptr(w), ctypes.c_int(w.shape[0]), ctypes.c_int(int(n_trotters)),
+            ctypes.c_int(common.optimize_flag(optimize)), ctypes.c_ulonglong(int(seed)), ptr(G), ptr(beta),
+            ctypes.c_int(len(G)), ctypes.byref(rid)))
         self._shape[rid.value] = (int(n_trotters), W.shape[0], 0)
         return rid.value
 
