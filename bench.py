@@ -449,6 +449,234 @@ def run_batched(args, world):
     print(json.dumps(line), flush=True)
 
 
+class BipartiteTask(ctypes.Structure):
+    """Mirror of sq103_bipartite_task (include/sqaod_gb300.h)."""
+    _fields_ = [("J", ctypes.c_void_p), ("h0", ctypes.c_void_p), ("h1", ctypes.c_void_p), ("q0", ctypes.c_void_p),
+                ("q1", ctypes.c_void_p), ("F0", ctypes.c_void_p), ("F1", ctypes.c_void_p),
+                ("trace", ctypes.c_void_p), ("accepted", ctypes.c_void_p), ("G", ctypes.c_void_p),
+                ("beta", ctypes.c_void_p), ("Gs", ctypes.c_float), ("betas", ctypes.c_float),
+                ("seed", ctypes.c_uint64), ("step0", ctypes.c_uint32), ("N0", ctypes.c_int), ("N1", ctypes.c_int),
+                ("m", ctypes.c_int), ("algo", ctypes.c_int), ("nSteps", ctypes.c_int)]
+
+
+def _timed_steps(stream, flush, K, fn):
+    """K calls of fn(i), each bracketed by CUDA events on `stream`, with a
+    512 MB write between them (L2 flush, untimed); returns per-call ms."""
+    import torch
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    for i in range(K):
+        flush.fill_(i & 0xff)
+        starts[i].record(stream)
+        fn(i)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def run_bipartite(args, world):
+    """Bipartite SQA coloring, N0 = N1 = 1024, m = 64, beta = 50, the 619-step
+    schedule sampled evenly; b0, b1, W iid uniform[-1, 1] under
+    np.random.seed(0).  value = trials/s of the device-resident step (kernel
+    layer, L2 flushed between steps); the field GEMMs (two per step) are also
+    timed alone, since they carry the step's arithmetic."""
+    import torch
+    import sqaod_gb300 as sq
+    from sqaod_gb300 import _lib
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    N0, N1, m = 1024, 1024, 64
+    rs = np.random.RandomState(0)
+    b0 = rs.uniform(-1, 1, N0).astype(np.float32)
+    b1 = rs.uniform(-1, 1, N1).astype(np.float32)
+    W = rs.uniform(-1, 1, (N1, N0)).astype(np.float32)
+
+    def T(a, dt=torch.float32):
+        return torch.from_numpy(a).to(dev) if isinstance(a, np.ndarray) else torch.empty(a, dtype=dt, device=dev)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    dW, db0, db1 = T(W), T(b0), T(b1)
+    J, h0, h1 = T(N1 * N0), T(N0), T(N1)
+    c32, c64, scr = T(1), T(1, torch.float64), T(N0 + N1, torch.float64)
+    q0, q1 = T(m * N0, torch.int8), T(m * N1, torch.int8)
+    F0, F1 = T(m * N0), T(m * N1)
+    acc = torch.zeros(1, dtype=torch.int64, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    seed = 1000
+    assert L.sq103_bipartite_hamiltonian(P(db0), P(db1), P(dW), N0, N1, 0, P(h0), P(h1), P(J), P(c32), P(c64),
+                                         P(scr), sp) == 0
+    assert L.sq103_randomize_spins(P(q0), N0, m, ctypes.c_uint64(seed), ctypes.c_uint32(0), 0, sp) == 0
+    assert L.sq103_randomize_spins(P(q1), N1, m, ctypes.c_uint64(seed), ctypes.c_uint32(0), 1, sp) == 0
+    sched = schedule()
+    K, Wm = args.steps, args.warmup
+    idx = np.linspace(0, len(sched) - 1, max(K, 1)).round().astype(int)
+    step = [1]
+
+    def launch(G):
+        t = BipartiteTask(J=J.data_ptr(), h0=h0.data_ptr(), h1=h1.data_ptr(), q0=q0.data_ptr(), q1=q1.data_ptr(),
+                          F0=F0.data_ptr(), F1=F1.data_ptr(), trace=None, accepted=acc.data_ptr(), G=None,
+                          beta=None, Gs=G, betas=BETA, seed=seed, step0=step[0], N0=N0, N1=N1, m=m, algo=1,
+                          nSteps=1)
+        rc = L.sq103_bipartite_anneal(ctypes.byref(t), sp)
+        if rc != 0:
+            raise RuntimeError("sq103_bipartite_anneal failed: %d" % rc)
+        step[0] += 1
+
+    for i in range(Wm):
+        launch(sched[i % len(sched)])
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(stream, flush, K, lambda i: launch(sched[idx[i]]))
+        gemm_ms = _timed_steps(stream, flush, K, lambda i: (
+            L.sq103_bipartite_fields(P(J), N0, N1, P(q0), 1, P(F1), m, sp),
+            L.sq103_bipartite_fields(P(J), N0, N1, P(q1), 0, P(F0), m, sp)))
+    t_ms = float(np.mean(ms))
+    g_ms = float(np.mean(gemm_ms)) / 2
+    trials = float(N0 + N1) * m
+    value = trials * world / (t_ms / 1e3)
+    gemm_flops = 2.0 * m * N0 * N1
+    sm_peak_tflops = 152 * 128 * 2 * 2.07e9 / 1e12  # fp32 FMA lanes x max SM clock
+    # end to end through the Python solver API, one whole anneal
+    G_all = np.array(sched, np.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a = sq.cuda.bipartite_graph_annealer(b0, b1, W, sq.minimize, n_trotters=m, algorithm="coloring")
+    a.seed(seed)
+    a.prepare()
+    a.randomize_spin()
+    a.anneal(G_all, BETA)
+    a.make_solution()
+    E = a.get_E()
+    e2e_s = time.perf_counter() - t0
+    nS = len(G_all)
+    del a
+    # CPU: the restated reference bipartite annealer, a bounded sample of steps
+    from oracle import oracle_ctypes as orc
+    hh0, hh1, JJ, cc = orc.bg_hamiltonian(b0, b1, W)
+    ref = orc.BipartiteAnnealerRef(hh0.astype(np.float32), hh1.astype(np.float32), JJ.astype(np.float32),
+                                   float(cc), m, n_workers=0)
+    ref.seed(0)
+    ref.randomize_spin()
+    t1 = time.perf_counter()
+    n_cpu = 0
+    while time.perf_counter() - t1 < 3.0:
+        ref.anneal_one_step(orc.ALGO_COLORING, sched[idx[n_cpu % len(idx)]], BETA)
+        n_cpu += 1
+    cpu_s = time.perf_counter() - t1
+    line = {"metric": "spin-flip trials/s (bipartite SQA coloring, N0=N1=%d m=%d)" % (N0, m), "value": value,
+            "unit": "trials/s", "n_gpus": world, "steps": K, "warmup": Wm, "ms_per_step": t_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (b0, b1, W iid uniform[-1,1], np.random.seed(0))",
+            "config": {"workload": "bipartite SQA coloring N0=N1=%d m=%d beta=50 G=5*0.99^k (619-step schedule "
+                                   "sampled evenly)" % (N0, m), "l2": "flushed between timed steps (512 MB write)"},
+            "gpu_launches": K * 6,
+            "roofline": {"bound": "fp32 simt", "kernel": "bip_field_kernel (field GEMM, 2 per step)",
+                         "achieved": gemm_flops / (g_ms / 1e3) / 1e12, "peak": sm_peak_tflops, "unit": "TFLOP/s",
+                         "frac": gemm_flops / (g_ms / 1e3) / 1e12 / sm_peak_tflops, "traffic": None,
+                         "peak_source": "nominal fp32 FMA rate at the maximum SM clock",
+                         "gemm_ms": g_ms, "gemm_share_of_step": 2 * g_ms / t_ms},
+            "e2e": {"value": trials * nS / e2e_s, "unit": "trials/s", "steps": nS, "seconds": e2e_s,
+                    "h2d_bytes_per_step": int((W.nbytes + b0.nbytes + b1.nbytes + 2 * G_all.nbytes) / nS),
+                    "d2h_bytes_per_step": int((m * (N0 + N1) + 4 * len(E)) / nS), "min_E": float(np.min(E))},
+            "cpu_baseline": {"value": trials * n_cpu / cpu_s, "unit": "trials/s", "cores": ref.workers,
+                             "kind": "port", "sample": "%d annealOneStep of the same instance, %.1f s" % (n_cpu, cpu_s)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def bf_problem(N=32, seed=0):
+    """W N x N, upper triangle iid integers uniform in [-8, 8] under
+    np.random.seed(seed), mirrored; stored fp32."""
+    rs = np.random.RandomState(seed)
+    U = np.triu(rs.randint(-8, 9, (N, N)))
+    return (U + np.triu(U, 1).T).astype(np.float32)
+
+
+def run_bf(args, world):
+    """Dense brute-force search over all 2^32 states of an N = 32 integer
+    QUBO (kernel layer: sq103_dense_bf_range over [0, 2^32), min pass and
+    argmin collection, then the FP64 re-evaluation of the argmins)."""
+    import torch
+    import sqaod_gb300 as sq
+    from sqaod_gb300 import _lib
+    L = _lib.lib()
+    L.sq103_bf_workspace_bytes.restype = ctypes.c_size_t
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    N = 32
+    W = bf_problem(N)
+    dW = torch.from_numpy(W).to(dev)
+    ws = torch.empty(int(L.sq103_bf_workspace_bytes(N)), dtype=torch.uint8, device=dev)
+    cap = 1 << 16
+    cand = torch.empty(cap, dtype=torch.int64, device=dev)
+    E64 = torch.empty(cap, dtype=torch.float64, device=dev)
+    count = ctypes.c_int()
+    Emin = ctypes.c_float()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    nStates = 1 << N
+
+    def search(i):
+        rc = L.sq103_dense_bf_range(ctypes.c_void_p(dW.data_ptr()), N, ctypes.c_uint64(0), ctypes.c_uint64(nStates),
+                                    ctypes.c_float(0.0), ctypes.c_void_p(ws.data_ptr()),
+                                    ctypes.c_void_p(cand.data_ptr()), cap, ctypes.byref(count), ctypes.byref(Emin), sp)
+        if rc != 0:
+            raise RuntimeError("sq103_dense_bf_range failed: %d" % rc)
+        n = min(count.value, cap)
+        if n:
+            L.sq103_dense_bf_refine(ctypes.c_void_p(dW.data_ptr()), N, ctypes.c_void_p(cand.data_ptr()), n,
+                                    ctypes.c_void_p(E64.data_ptr()), sp)
+
+    K, Wm = args.steps, args.warmup
+    for i in range(Wm):
+        search(i)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        ms = _timed_steps(stream, flush, K, search)
+    t_ms = float(np.mean(ms))
+    value = nStates * world / (t_ms / 1e3)
+    # the reference formulation's arithmetic per state: the X.W GEMM row plus the row dot (2N^2 + 2N)
+    ref_flops = (2.0 * N * N + 2.0 * N) * nStates
+    # end to end: the Python searcher (set_qubo uploads W, search, argmins back)
+    t0 = time.perf_counter()
+    s = sq.cuda.dense_graph_bf_searcher(W, sq.minimize)
+    s.search()
+    E_api = s.get_E()
+    x_api = s.get_x()
+    e2e_s = time.perf_counter() - t0
+    del s
+    # CPU: the restated reference searcher's arithmetic (X.W per state) on a 2^25-state sample
+    from oracle import oracle_ctypes as orc
+    tile, n_tiles = 1024, 1 << 15
+    t1 = time.perf_counter()
+    orc.dg_bf_sweep_tiles(W, 0, tile, n_tiles, 0)
+    cpu_s = time.perf_counter() - t1
+    line = {"metric": "states/s (dense brute-force search, N=32)", "value": value, "unit": "states/s",
+            "n_gpus": world, "steps": K, "warmup": Wm, "ms_per_step": t_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (W 32x32, iid integers uniform[-8, 8] upper triangle mirrored, np.random.seed(0))",
+            "config": {"workload": "dense BF N=32, all 2^32 states per step", "l2": "flushed between timed steps",
+                       "Emin": float(Emin.value), "argmins": int(count.value)},
+            "gpu_launches": K * 5,
+            "roofline": {"bound": "issue (table lookups, no GEMM)", "achieved": None, "peak": None, "unit": None,
+                         "frac": None, "traffic": None,
+                         "reference_equivalent_tflops": ref_flops / (t_ms / 1e3) / 1e12,
+                         "note": "the reference evaluates X.W per tile (2N^2+2N flops per state); this search "
+                                 "uses 2^14-entry tables and does ~3 lookups and adds per state"},
+            "e2e": {"value": nStates / e2e_s, "unit": "states/s", "seconds": e2e_s, "h2d_bytes_per_step": W.nbytes,
+                    "d2h_bytes_per_step": int(len(E_api) * 4 + np.asarray(x_api).size),
+                    "Emin": float(np.min(E_api))},
+            "cpu_baseline": {"value": tile * n_tiles / cpu_s, "unit": "states/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "%d states (tiles of %d from x = 0), %.1f s" % (
+                                 tile * n_tiles, tile, cpu_s)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -479,8 +707,9 @@ def main():
     ap.add_argument("--size", default="%d,%d" % (N_SPINS, N_TROTTERS),
                     help="N,m of the instance (smaller cases are for profiling captures only)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
-    ap.add_argument("--mode", default="sweep", choices=["sweep", "batched", "served"],
-                    help="sweep: the headline dense sweep; batched: 1024 uneven instances; served: mixed stream")
+    ap.add_argument("--mode", default="sweep", choices=["sweep", "batched", "served", "bipartite", "bf"],
+                    help="sweep: the headline dense sweep; batched: 1024 uneven instances; served: mixed stream; "
+                         "bipartite: N0=N1=1024 m=64 sweep; bf: dense brute force N=32")
     ap.add_argument("--window", type=float, default=20.0, help="served mode: seconds per path")
     ap.add_argument("--slots", type=int, default=512, help="served mode: concurrent instances per kind")
     ap.add_argument("--large", type=int, default=4, help="served mode: concurrent whole-GPU instances")
@@ -500,7 +729,8 @@ def main():
     torch.cuda.set_device(local)
     if args.mode != "sweep":
         if rank == 0:
-            (run_batched if args.mode == "batched" else run_served)(args, world)
+            {"batched": run_batched, "served": run_served, "bipartite": run_bipartite, "bf": run_bf}[args.mode](
+                args, world)
         return
     dist = None
     if world > 1:

@@ -749,6 +749,8 @@ orc_bga *orc_bga_new(int N0, int N1, int m, int nWorkers) {
     return a;
 }
 
+int orc_bga_workers(const orc_bga *a) { return a->nw; }
+
 void orc_bga_free(orc_bga *a) {
     if (!a) return;
     free(a->h0); free(a->h1); free(a->J); free(a->q0); free(a->q1); free(a->dE); free(a->rng);

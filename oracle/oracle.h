@@ -120,6 +120,7 @@ void orc_dga_energy(const orc_dga *a, double *E);
 typedef struct orc_bga orc_bga;
 orc_bga *orc_bga_new(int N0, int N1, int m, int nWorkers);
 void orc_bga_free(orc_bga *a);
+int orc_bga_workers(const orc_bga *a);
 void orc_bga_set_hamiltonian(orc_bga *a, const float *h0, const float *h1, const float *J, float c);
 void orc_bga_seed(orc_bga *a, unsigned long long seed);
 void orc_bga_randomize(orc_bga *a);

@@ -266,6 +266,10 @@ class BipartiteAnnealerRef:
             lib().orc_bga_free(ctypes.c_void_p(self._h))
             self._h = None
 
+    @property
+    def workers(self):
+        return lib().orc_bga_workers(ctypes.c_void_p(self._h))
+
     def seed(self, s):
         lib().orc_bga_seed(ctypes.c_void_p(self._h), ctypes.c_ulonglong(s))
 

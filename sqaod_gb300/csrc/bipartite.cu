@@ -16,7 +16,7 @@
 // sa_naive: per trotter, (N0+N1) m trials at x = hi(w0 (N0+N1)) of
 // philox((t, y, step, 0x34)) (CPUBipartiteGraphAnnealer.cpp:446-480).
 // The naive fields are a fixed-order block reduction of one J row or column.
-#include "spin_gemm.cuh"
+#include "bip_field.cuh"
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
@@ -147,12 +147,13 @@ __global__ void __launch_bounds__(256) bip_naive(sq103_bipartite_task T, int s) 
 
 // Persistent batch of bipartite instances (coloring / sa_coloring): one CTA
 // runs a whole annealOneStep of one instance -- both half-step field GEMMs
-// (the spin_gemm tiles, looped by the CTA) and the colour phases -- for steps
+// (the bip_field tiles, looped by the CTA) and the colour phases -- for steps
 // [pos[i], pos[i] + stepsPerLaunch) of its schedule.  Same arithmetic as
 // sq103_bipartite_anneal, so results are bit-identical.
 __global__ void __launch_bounds__(256) bip_batch_persistent(const sq103_bipartite_task *tasks, const int *nTasksDev,
                                                             int nTasksHost, const int *order, int *pos, int *queue,
                                                             int stepsPerLaunch) {
+    extern __shared__ __align__(16) float smem[];  // kBipFieldSmem bytes: field tile staging
     __shared__ int item;
     const int nTasks = nTasksDev ? *nTasksDev : nTasksHost;
     for (;;) {
@@ -177,14 +178,15 @@ __global__ void __launch_bounds__(256) bip_batch_persistent(const sq103_bipartit
                 int8_t *qA = side ? T.q1 : T.q0;
                 float *F = side ? T.F1 : T.F0;
                 const float *h = side ? T.h1 : T.h0;
-                for (int ty = 0; ty < m; ty += 64)
-                    for (int tx = 0; tx < Ns; tx += 64) {
+                for (int ty = 0; ty < m; ty += kBipTileM)
+                    for (int tx = 0; tx < Ns; tx += kBipTileN) {
                         if (side)
-                            spin_gemm_tile<true, float>(T.q0, T.N0, T.J, T.N0, F, T.N1, m, T.N1, T.N0, ty, tx);
+                            bip_field_tile<true, false, float>(T.q0, T.N0, T.J, T.N0, F, T.N1, m, T.N1, T.N0, ty,
+                                                               tx, smem);
                         else
-                            spin_gemm_tile<false, float>(T.q1, T.N1, T.J, T.N0, F, T.N0, m, T.N0, T.N1, ty, tx);
+                            bip_field_tile<false, false, float>(T.q1, T.N1, T.J, T.N0, F, T.N0, m, T.N0, T.N1, ty,
+                                                                tx, smem);
                     }
-                __syncthreads();
                 const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
                 for (int ph = 0; ph < 3; ++ph) {
                     int yb, ys, cnt;
@@ -229,8 +231,12 @@ extern "C" SQ103_API int sq103_bipartite_batch_launch(const sq103_bipartite_task
                                                       const int *d_nTasks, const int *d_order, int *d_pos,
                                                       int *d_queue, int stepsPerLaunch, int grid, void *stream) {
     if (grid <= 0) return kErrBadShape;
-    bip_batch_persistent<<<grid, 256, 0, (cudaStream_t)stream>>>(d_tasks, d_nTasks, nTasks, d_order, d_pos, d_queue,
-                                                                 stepsPerLaunch);
+    // the field tiles' 48 KB plus the kernel's own words exceed the default limit
+    cudaError_t e = cudaFuncSetAttribute(bip_batch_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kBipFieldSmem);
+    if (e != cudaSuccess) return (int)e;
+    bip_batch_persistent<<<grid, 256, kBipFieldSmem, (cudaStream_t)stream>>>(d_tasks, d_nTasks, nTasks, d_order,
+                                                                             d_pos, d_queue, stepsPerLaunch);
     return (int)cudaGetLastError();
 }
 

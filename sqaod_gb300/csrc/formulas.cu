@@ -14,15 +14,15 @@
 //   field_gemm (field_gemm.cuh): the dense field refresh F = q J (fp32 partial
 //     sums over 32-wide k chunks, compensated fp32 sum of the chunks) and the
 //     dense energy row sums (double-float accumulation of every product);
-//   spin_gemm (spin_gemm.cuh): the bipartite half-step fields (FP64 sum of fp32
-//     chunk partials) and the bipartite energy row sums (FP64).
+//   bip_field (bip_field.cuh): the bipartite half-step fields and energy row
+//     sums, K split over the 8 warps of a CTA, groups folded in a fixed order.
 // All are deterministic: the order of every addition is fixed.
 #include <cstdio>
 #include <mutex>
 #include <type_traits>
 
 #include "field_gemm.cuh"
-#include "spin_gemm.cuh"
+#include "bip_field.cuh"
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
@@ -115,14 +115,14 @@ __global__ void bg_hamiltonian_cols(const float *W, int N0, int N1, float sign, 
     colc[j] = -0.5 * bj;
 }
 
-// ------------------------------------------------------------ spin GEMM
-// (spin_gemm.cuh)
+// ------------------------------------------------------- bipartite GEMM
+// (bip_field.cuh)
 
-template <bool TRANS_B, typename OutT>
-static void launch_spin_gemm(const int8_t *A, int lda, const float *B, int ldb, OutT *C, int ldc, int M,
-                             int Nn, int K, cudaStream_t s) {
-    dim3 grid((Nn + 63) / 64, (M + 63) / 64);
-    spin_gemm_kernel<TRANS_B, OutT><<<grid, 256, 0, s>>>(A, lda, B, ldb, C, ldc, M, Nn, K);
+template <bool TRANS_B, bool EXACT, typename OutT>
+static void launch_bip_field(const int8_t *A, int lda, const float *B, int ldb, OutT *C, int ldc, int M, int Nn,
+                             int K, cudaStream_t s) {
+    dim3 grid((Nn + kBipTileN - 1) / kBipTileN, (M + kBipTileM - 1) / kBipTileM);
+    bip_field_kernel<TRANS_B, EXACT, OutT><<<grid, 256, kBipFieldSmem, s>>>(A, lda, B, ldb, C, ldc, M, Nn, K);
 }
 
 // ------------------------------------------------------------ energies
@@ -220,9 +220,9 @@ SQ103_API int sq103_bipartite_fields(const float *J, int N0, int N1, const int8_
                            void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (side == 1)  // F1[y][i] = sum_j J[i][j] q0[y][j]
-        launch_spin_gemm<true, float>(qFixed, N0, J, N0, F, N1, m, N1, N0, s);
+        launch_bip_field<true, false, float>(qFixed, N0, J, N0, F, N1, m, N1, N0, s);
     else  // F0[y][j] = sum_i q1[y][i] J[i][j]
-        launch_spin_gemm<false, float>(qFixed, N1, J, N0, F, N0, m, N0, N1, s);
+        launch_bip_field<false, false, float>(qFixed, N1, J, N0, F, N0, m, N0, N1, s);
     return (int)cudaGetLastError();
 }
 
@@ -239,7 +239,7 @@ SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const floa
                            const int8_t *q0, const int8_t *q1, int N0, int N1, int m, int maximize,
                            double *r_scratch, double *E64, float *E32, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    launch_spin_gemm<true, double>(q0, N0, J, N0, r_scratch, N1, m, N1, N0, s);
+    launch_bip_field<true, true, double>(q0, N0, J, N0, r_scratch, N1, m, N1, N0, s);
     bg_energy_finish<<<m, 256, 0, s>>>(q0, q1, N0, N1, h0, h1, r_scratch, c64, maximize ? -1. : 1., E64,
                                        E32);
     return (int)cudaGetLastError();
