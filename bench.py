@@ -449,6 +449,15 @@ def run_batched(args, world):
     print(json.dumps(line), flush=True)
 
 
+def _profiled_traffic(key):
+    """DRAM bytes per launch of a kernel, from the ncu capture summarised in profiles/."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key, {}).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
 class BipartiteTask(ctypes.Structure):
     """Mirror of sq103_bipartite_task (include/sqaod_gb300.h)."""
     _fields_ = [("J", ctypes.c_void_p), ("h0", ctypes.c_void_p), ("h1", ctypes.c_void_p), ("q0", ctypes.c_void_p),
@@ -576,7 +585,8 @@ def run_bipartite(args, world):
             "gpu_launches": K * 6,
             "roofline": {"bound": "fp32 simt", "kernel": "bip_field_kernel (field GEMM, 2 per step)",
                          "achieved": gemm_flops / (g_ms / 1e3) / 1e12, "peak": sm_peak_tflops, "unit": "TFLOP/s",
-                         "frac": gemm_flops / (g_ms / 1e3) / 1e12 / sm_peak_tflops, "traffic": None,
+                         "frac": gemm_flops / (g_ms / 1e3) / 1e12 / sm_peak_tflops,
+                         "traffic": _profiled_traffic("bip_field_kernel N0=N1=%d m=%d" % (N0, m)),
                          "peak_source": "nominal fp32 FMA rate at the maximum SM clock",
                          "gemm_ms": g_ms, "gemm_share_of_step": 2 * g_ms / t_ms},
             "e2e": {"value": trials * nS / e2e_s, "unit": "trials/s", "steps": nS, "seconds": e2e_s,
@@ -856,12 +866,7 @@ def main():
                "sample": "1 annealOneStep (1,048,576 trials) at G=5.0 of the same instance, %.1f s" % dt}
 
     if rank == 0:
-        traffic = None
-        try:
-            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-                traffic = json.load(f).get("dense_sweep_multi N=%d m=%d" % (N, m), {}).get("dram_bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+        traffic = _profiled_traffic("dense_sweep_multi N=%d m=%d" % (N, m))
         line = {"metric": "spin-flip trials/s (dense SQA coloring, N=%d m=%d)" % (N, m), "value": value,
                 "unit": "trials/s", "n_gpus": world, "steps": K, "warmup": Wm, "ms_per_step": t_ms / K,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
