@@ -829,13 +829,12 @@ def main():
         raise RuntimeError("sweep kernel reported device status %d" % int(status.item()))
     kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = float(sum(kernel_ms))
-    if dist:
-        tt = torch.tensor([t_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    accepted = (acc_hist[1:] - acc_hist[:-1]).cpu().numpy().astype(np.float64)
+    # replicas: every rank ran its own instance; the job rate is all ranks'
+    # trials over the slowest rank's time
+    from sqaod_gb300.shard import replica_throughput
     trials = float(N) * m * K
-    value = trials * world / (t_ms / 1e3)
+    value, t_ms = replica_throughput(t_ms, trials, device=dev)
+    accepted = (acc_hist[1:] - acc_hist[:-1]).cpu().numpy().astype(np.float64)
     alg_bytes = accepted * 4.0 * N + 10.0 * N * m
     achieved_gbs = float(alg_bytes.sum()) / (t_ms / 1e3) / 1e9
     peak, peak_kind = peaks()

@@ -306,6 +306,12 @@ SQ103_API int sq103_dg_bf_make_solution(void *handle);
 /* one tile; *done = 1 when the whole range is searched; curXEnd may be NULL */
 SQ103_API int sq103_dg_bf_search_range(void *handle, unsigned long long *curXEnd, int *done);
 SQ103_API int sq103_dg_bf_search(void *handle);
+/* No counterpart in the reference (multi-GPU sharding): search the packed
+ * states [xBegin, xEnd) after prepare(), merged into the searcher's result;
+ * the ranges one searcher is given must ascend.  get_E64: the exact FP64
+ * minimum found so far (signed for the optimisation direction). */
+SQ103_API int sq103_dg_bf_search_subrange(void *handle, unsigned long long xBegin, unsigned long long xEnd);
+SQ103_API int sq103_dg_bf_get_E64(void *handle, double *E);
 
 SQ103_API int sq103_bg_bf_new(void **handle);
 SQ103_API int sq103_bg_bf_delete(void *handle);

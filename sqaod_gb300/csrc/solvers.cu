@@ -892,6 +892,19 @@ public:
     }
     double EminExact() const { return om_ == sq::optMaximize ? -res_.Emin : res_.Emin; }
 
+    // one shard of a multi-GPU search: searches [b, e) after prepare() (ranges
+    // of one searcher in ascending order), merged into the running result
+    void searchSubrange(uint64_t b, uint64_t e) {
+        throwErrorIfNotPrepared();
+        throwErrorIf(b > e || e > xMax_, "range [%llu, %llu) is outside [0, 2^%d).", (unsigned long long)b,
+                     (unsigned long long)e, N_);
+        throwErrorIf(b < x_, "ranges must be searched in ascending order.");
+        clearState(solSolutionAvailable);
+        const uint64_t chunk = 1ull << 34;
+        for (uint64_t c = b; c < e; c += chunk) runRange(c, std::min<uint64_t>(e, c + chunk));
+        x_ = e;
+    }
+
 private:
     // one range in ascending order; splits itself when the candidates overflow
     void runRange(uint64_t b, uint64_t e) {

@@ -411,6 +411,18 @@ class DenseGraphBFSearcher(_Handle):
     def search(self):
         self._call('search')
 
+    def search_subrange(self, x_begin, x_end):
+        """Searches the packed states [x_begin, x_end) after prepare() (one shard of
+        a multi-GPU search; the ranges given to one searcher must ascend).  No
+        counterpart in the reference."""
+        self._call('search_subrange', ctypes.c_ulonglong(int(x_begin)), ctypes.c_ulonglong(int(x_end)))
+
+    def get_E64(self):
+        """Exact FP64 minimum found so far (negated for maximize)."""
+        e = ctypes.c_double()
+        self._call('get_E64', ctypes.byref(e))
+        return e.value
+
 
 class BipartiteGraphBFSearcher(_Handle):
     """Bipartite-graph brute-force searcher (sqaodpy/sqaod/common/bipartite_graph_bf_searcher_base.py)."""

@@ -526,6 +526,28 @@ def test_bipartite_bf_golden(sq, orc, golden):
     assert [(tuple(a), tuple(b)) for a, b in s2.get_x()] == [(tuple(a), tuple(b)) for a, b in s.get_x()]
 
 
+def test_dense_bf_shards_merge_to_whole_search(sq):
+    """Sub-range searches (the shards of a multi-GPU search) merged on the host
+    equal one search of the whole range: FP64 minimum and minimiser list."""
+    from sqaod_gb300 import shard
+    rng = np.random.default_rng(3)
+    U = np.triu(rng.integers(-8, 9, (20, 20)))
+    W = (U + np.triu(U, 1).T).astype(np.float32)
+    for optimize in (sq.minimize, sq.maximize):
+        parts = [shard.gpu_shard_search(W, optimize, *shard.shard_range(1 << 20, r, 3), 1024) for r in range(3)]
+        E, xs = shard.merge_shards(parts, 1024)
+        s = sq.cuda.dense_graph_bf_searcher(W, optimize, tile_size=1024)
+        s.search()
+        E_all = s.get_E64()
+        assert (-E if optimize is sq.maximize else E) == E_all
+        assert xs.tolist() == [shard.pack_bits(x) for x in s.get_x()]
+    s = sq.cuda.dense_graph_bf_searcher(W)
+    s.prepare()
+    s.search_subrange(16, 64)
+    with pytest.raises(RuntimeError):  # ranges must ascend
+        s.search_subrange(0, 8)
+
+
 def test_bf_known_answers(sq):
     N = 8
     for W, om, E, x in ((np.ones((N, N)), sq.minimize, 0., 0), (-np.ones((N, N)), sq.minimize, -64., 1),
