@@ -6,18 +6,22 @@ N = 4096 spins, m = 256 Trotter replicas, W symmetric uniform[-1, 1] drawn
 like sqaod's generate_random_symmetric_W under np.random.seed(0) (diagonal
 kept), algorithm = coloring, beta = 50, G = 5.0 * 0.99^k for the 619 steps
 k with G > 0.01.  A "step" is one annealOneStep (N * m = 1,048,576 Metropolis
-trials).  The K timed steps sample the 619-step schedule evenly, so the
-acceptance mix matches a whole anneal.
+trials).  Each of the K timed units is what the solver runs per field-refresh
+period: one sweep launch of 8 consecutive steps, then the field refresh
+(--steps-per-launch 1: single-step launches without refresh).  The units start
+at positions spread evenly over the 619-step schedule, so the acceptance mix
+matches a whole anneal.
 
   value  : spin-flip trials/s of the device-resident sweep (kernel layer,
            inputs resident in HBM, CUDA events on the launching stream,
-           L2 flushed between timed steps with a 512 MB write)
+           L2 flushed between timed units with a 512 MB write)
   e2e    : the same metric through the solver-handle C ABI with host
            buffers, for one whole anneal as a user runs it: set_qubo (H2D of
            W), seed, prepare, randomize_spin, anneal over the 619-step
            schedule, make_solution, get_E and get_x (D2H)
-  roofline: HBM roofline of the sweep kernel: algorithmic bytes per launch
-           = A * 4N + 10 N m (A = accepted flips counted by the kernel)
+  roofline: HBM roofline of the sweep kernel (its own launch time, refresh
+           excluded): algorithmic bytes per step = A * 4N + 10 N m (A = accepted
+           flips counted by the kernel), summed over the launch's steps
   cpu_baseline: the reference CPU coloring annealer (restated with the
            reference's MT19937 and AVX2-order dot), OpenMP on all host cores
 
@@ -726,6 +730,9 @@ def main():
     ap.add_argument("--size", default="%d,%d" % (N_SPINS, N_TROTTERS),
                     help="N,m of the instance (smaller cases are for profiling captures only)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling captures)")
+    ap.add_argument("--steps-per-launch", type=int, default=8, choices=[1, 8],
+                    help="sweep mode: annealOneSteps per timed sweep launch (8: one field-refresh period, "
+                         "refresh included, as the solver runs them; 1: single-step launches, no refresh)")
     ap.add_argument("--mode", default="sweep", choices=["sweep", "batched", "served", "bipartite", "bf"],
                     help="sweep: the headline dense sweep; batched: 1024 uneven instances; served: mixed stream; "
                          "bipartite: N0=N1=1024 m=64 sweep; bf: dense brute force N=32")
@@ -785,30 +792,43 @@ def main():
     assert L.sq103_dense_field_refresh(P(dJ), N, P(q), P(F), N, m, sp) == 0
     sched = schedule()
     K, Wm = args.steps, args.warmup
-    idx = np.linspace(0, len(sched) - 1, max(K, 1)).round().astype(int)
+    spl = args.steps_per_launch
+    # timed iteration i: spl annealOneSteps from schedule position s0[i] (spread
+    # evenly over the schedule) in one sweep launch, then -- for spl = 8, one
+    # field-refresh period -- the refresh the solver runs after every 8 steps
+    s0 = np.linspace(0, len(sched) - spl, max(K, 1)).round().astype(int)
+    dG = torch.tensor(sched, dtype=torch.float32, device=dev)
+    dB = torch.full_like(dG, BETA)
 
     L.sq103_dense_ws_bytes.restype = ctypes.c_ulonglong
-    ws_bytes = int(L.sq103_dense_ws_bytes(N, m, 1))
+    ws_bytes = int(L.sq103_dense_ws_bytes(N, m, spl))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     multi = bool(L.sq103_dense_multicta_ok(N, m, 1))
+    refresh = spl == 8
 
-    def launch(G, step):
+    def launch(pos, step):
         t = DenseTask(J=dJ.data_ptr(), h=dh.data_ptr(), q=q.data_ptr(), F=F.data_ptr(), trace=None,
-                      accepted=acc.data_ptr(), G=None, beta=None, Gs=G, betas=BETA, status=status.data_ptr(),
-                      seed=seed, step0=step, N=N, m=m, ldJ=N, algo=1, nSteps=1, ws=ws.data_ptr(),
-                      wsBytes=ws_bytes, flags=0)
+                      accepted=acc.data_ptr(), G=dG.data_ptr() + 4 * pos, beta=dB.data_ptr() + 4 * pos, Gs=0.0,
+                      betas=BETA, status=status.data_ptr(), seed=seed, step0=step, N=N, m=m, ldJ=N, algo=1,
+                      nSteps=spl, ws=ws.data_ptr(), wsBytes=ws_bytes, flags=0)
         rc = L.sq103_dense_anneal(ctypes.byref(t), sp)
         if rc != 0:
             raise RuntimeError("sq103_dense_anneal failed: %d" % rc)
 
+    def do_refresh():
+        if refresh and L.sq103_dense_field_refresh(P(dJ), N, P(q), P(F), N, m, sp) != 0:
+            raise RuntimeError("sq103_dense_field_refresh failed")
+
     step = 1
     for i in range(Wm):
-        launch(sched[i % len(sched)], step)
-        step += 1
+        launch((i * spl) % (len(sched) - spl + 1), step)
+        do_refresh()
+        step += spl
     torch.cuda.synchronize()
     acc_hist = torch.zeros(K + 1, dtype=torch.int64, device=dev)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    mids = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     if dist:
         dist.barrier()
@@ -817,26 +837,28 @@ def main():
         wall0 = time.perf_counter()
         acc_hist[0].copy_(acc[0])
         for i in range(K):
-            flush.fill_(i & 0xff)  # L2 flush between timed steps (untimed)
+            flush.fill_(i & 0xff)  # L2 flush between timed iterations (untimed)
             starts[i].record(stream)
-            launch(sched[idx[i]], step)
-            ends[i].record(stream)
-            step += 1
+            launch(int(s0[i]), step)
+            mids[i].record(stream)
             acc_hist[i + 1].copy_(acc[0])
+            do_refresh()
+            ends[i].record(stream)
+            step += spl
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     if int(status.item()) != 0:
         raise RuntimeError("sweep kernel reported device status %d" % int(status.item()))
-    kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    t_ms = float(sum(kernel_ms))
+    t_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
+    sweep_ms = float(sum(a.elapsed_time(b) for a, b in zip(starts, mids)))
     # replicas: every rank ran its own instance; the job rate is all ranks'
     # trials over the slowest rank's time
     from sqaod_gb300.shard import replica_throughput
-    trials = float(N) * m * K
+    trials = float(N) * m * K * spl
     value, t_ms = replica_throughput(t_ms, trials, device=dev)
-    accepted = (acc_hist[1:] - acc_hist[:-1]).cpu().numpy().astype(np.float64)
-    alg_bytes = accepted * 4.0 * N + 10.0 * N * m
-    achieved_gbs = float(alg_bytes.sum()) / (t_ms / 1e3) / 1e9
+    accepted = (acc_hist[1:] - acc_hist[:-1]).cpu().numpy().astype(np.float64)  # per launch
+    alg_bytes = accepted * 4.0 * N + 10.0 * N * m * spl                          # per launch
+    achieved_gbs = float(alg_bytes.sum()) / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
 
     # -------- end to end through the solver-handle C ABI with host buffers: one
@@ -875,21 +897,27 @@ def main():
                          "over the 619-step schedule, %.1f s" % (n, dt)}
 
     if rank == 0:
-        traffic = _profiled_traffic("dense_sweep_multi N=%d m=%d" % (N, m))
+        traffic = _profiled_traffic("dense_sweep_multi N=%d m=%d steps=%d" % (N, m, spl))
         line = {"metric": "spin-flip trials/s (dense SQA coloring, N=%d m=%d)" % (N, m), "value": value,
-                "unit": "trials/s", "n_gpus": world, "steps": K, "warmup": Wm, "ms_per_step": t_ms / K,
+                "unit": "trials/s", "n_gpus": world, "steps": K * spl, "warmup": Wm * spl,
+                "ms_per_step": t_ms / (K * spl),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (sqaod generate_random_symmetric_W(%d, -1, 1), np.random.seed(0))" % N,
                 "config": {"workload": "dense SQA coloring N=%d m=%d beta=50 G=5*0.99^k (619-step " % (N, m) +
                                        "schedule sampled evenly over the timed steps)",
-                           "N": N, "m": m, "algorithm": "coloring", "l2": "flushed between timed steps (512 MB write)",
+                           "N": N, "m": m, "algorithm": "coloring",
+                           "timed_unit": ("%d annealOneSteps in one sweep launch + the field refresh the solver "
+                                          "runs every 8 steps" % spl) if refresh else
+                                         ("%d annealOneStep(s) per sweep launch, no refresh" % spl),
+                           "l2": "flushed between timed units (512 MB write)",
                            "kernel": "one CTA per trotter (cooperative)" if multi else "one CTA per instance",
                            "parallelism": "replicas" if world > 1 else "single instance"},
-                "e2e": e2e, "gpu_launches": K,
+                "e2e": e2e, "gpu_launches": K * (2 if refresh else 1),
                 "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
                              "frac": achieved_gbs / peak, "traffic": traffic, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": float(alg_bytes.mean()),
-                             "accepted_per_step": float(accepted.mean())},
+                             "steps_per_launch": spl, "sweep_ms_per_launch": sweep_ms / K,
+                             "accepted_per_step": float(accepted.mean()) / spl},
                 "cpu_baseline": cpu, "clocks": clk.summary(), "wall_s": wall}
         print(json.dumps(line), flush=True)
     if dist:
