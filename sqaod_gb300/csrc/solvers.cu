@@ -35,6 +35,26 @@ namespace sq103 {
 
 namespace sq = sqaod;
 
+// Exact W == W^T on the device (the host check of sqaodc/common/Common.cpp:97-104,
+// `!=` per element pair): each 32 x 32 tile on or below the diagonal is
+// compared with its mirror tile, staged transposed in shared memory.
+__global__ void sym_check_kernel(const float *W, int N, int ld, int *bad) {
+    __shared__ float t[32][33];
+    const int bx = blockIdx.x, by = blockIdx.y, tx = threadIdx.x, ty = threadIdx.y;
+    if (bx > by) return;
+    for (int j = ty; j < 32; j += 8) {
+        const int r = bx * 32 + j, c = by * 32 + tx;
+        t[j][tx] = (r < N && c < N) ? W[(size_t)r * ld + c] : 0.f;
+    }
+    __syncthreads();
+    int mismatch = 0;
+    for (int j = ty; j < 32; j += 8) {
+        const int r = by * 32 + j, c = bx * 32 + tx;
+        if (r < N && c < N && W[(size_t)r * ld + c] != t[tx][j]) mismatch = 1;
+    }
+    if (__syncthreads_or(mismatch) && tx == 0 && ty == 0) atomicOr(bad, 1);
+}
+
 class DeviceImpl : public sq::cuda::Device {
 public:
     explicit DeviceImpl(int devNo) { initialize(devNo < 0 ? 0 : devNo); }
@@ -91,19 +111,34 @@ public:
 
     void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
         throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
-        throwErrorIf(!sq::isSymmetric(W), "%s, Matrix is not symmetric.", __func__);
+        // the exact symmetry check (Common.cpp:97-104) runs on the uploaded copy,
+        // before any state changes
+        const int N = W.rows;
+        DevBuf<float> dW;
+        dW.ensure((size_t)N * N);
+        upload(dW.p, N, W);
+        throwErrorIf(!deviceSymmetric(dW.p, N, N), "%s, Matrix is not symmetric.", __func__);
         clearState(solProblemSet);
-        N_ = W.rows;
+        N_ = N;
         m_ = N_ / 4;
         om_ = om;
         allocProblem();
-        DevBuf<float> dW;
-        dW.ensure((size_t)N_ * N_);
-        upload(dW.p, N_, W);
         SQ_CHECK(sq103_dense_hamiltonian(dW.p, N_, N_, om == sq::optMaximize, d_h_.p, d_J_.p, ldJ_, d_c_.p,
                                          d_c64_.p, d_scratchN_.p, st_.get()));
         st_.sync();
         setState(solProblemSet);
+    }
+
+    bool deviceSymmetric(const float *dW, int N, int ld) {
+        d_flag_.ensure(1);
+        SQ_CHECK(cudaMemsetAsync(d_flag_.p, 0, sizeof(int), st_.get()));
+        const int nT = (N + 31) / 32;
+        sym_check_kernel<<<dim3(nT, nT), dim3(32, 8), 0, st_.get()>>>(dW, N, ld, d_flag_.p);
+        SQ_CHECK(cudaGetLastError());
+        int bad = 0;
+        SQ_CHECK(cudaMemcpyAsync(&bad, d_flag_.p, sizeof(int), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        return bad == 0;
     }
 
     void setHamiltonian(const Vector &h, const Matrix &J, float c) override {
@@ -407,7 +442,7 @@ private:
     int refreshPeriod_ = 8, stepsSinceRefresh_ = 0;
     int kernelFlags_ = 0;
     DevBuf<unsigned char> d_ws_;
-    DevBuf<int> d_status_;
+    DevBuf<int> d_status_, d_flag_;
 
 public:
     void setKernel(int flags) {

@@ -83,6 +83,22 @@ def test_dense_set_qubo_triangular_input(sq):
             assert rel_close(a.get_E(), b.get_E(), 1e-6)
 
 
+def test_dense_set_qubo_rejects_asymmetric(sq):
+    """The exact symmetry check runs on the device copy, before any state
+    changes: an asymmetric W is rejected and the previous problem stays."""
+    rng = np.random.default_rng(9)
+    S = rand_sym(rng, 70)
+    a = sq.cuda.dense_graph_annealer(S)
+    h0, J0, c0 = a.get_hamiltonian()
+    for r, c in ((3, 60), (69, 0), (33, 32)):  # inside, corner and diagonal-adjacent tiles
+        B = S.copy()
+        B[r, c] += 0.5
+        with pytest.raises(RuntimeError, match="symmetric"):
+            a.set_qubo(B)
+        h1, J1, c1 = a.get_hamiltonian()
+        assert np.array_equal(h0, h1) and np.array_equal(J0, J1) and c0 == c1
+
+
 def test_dense_energy_all_states_golden(sq, golden):
     W, X = golden["dg_r8_W"].astype(np.float32), golden["dg_r8_X"]
     a = sq.cuda.dense_graph_annealer(W)
