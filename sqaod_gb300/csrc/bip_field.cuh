@@ -59,8 +59,18 @@ __device__ __forceinline__ void bip_field_tile(const int8_t *A, int lda, const f
         for (int b = 0; b < 4; ++b) s[a][b] = c[a][b] = 0.f;
 
     float ra[16], rb[32];
+    const bool rowsIn = y0 + 16 <= M && n0 + 32 <= Nn;
     auto load = [&](int ch) {
         const int k0 = ch << 5, k = k0 + lane;
+        if (rowsIn && k0 + 32 <= K) {  // the whole chunk is inside: no bounds checks
+            const int8_t *Ap = A + (size_t)y0 * lda + k;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) ra[i] = (float)Ap[(size_t)i * lda];
+            const float *Bp = TRANS_B ? Bm + (size_t)n0 * ldb + k : Bm + (size_t)k0 * ldb + n0 + lane;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) rb[j] = Bp[(size_t)j * ldb];
+            return;
+        }
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             const int y = y0 + i;
