@@ -40,8 +40,36 @@ __global__ void __launch_bounds__(256) field_gemm_kernel(const int8_t *A, int ld
     const int ar = tid >> 2, ak = (tid & 3) * 8;
     const int bk = tid >> 3, bc = (tid & 7) * 4;
     float la[8], lb[8];
+    // chunks inside the matrices take vector loads without bounds checks (same values)
+    const bool inside = y0 + 64 <= M && n0 + 64 <= Nn;
+    const bool vecA = !(lda & 7) && !(reinterpret_cast<uintptr_t>(A) & 7);
+    const bool vecB = !(ldb & 3) && !(reinterpret_cast<uintptr_t>(B) & 15);
     auto load = [&](int k0) {
         const int y = y0 + ar;
+        if (inside && k0 + 32 <= K) {
+            if (vecA) {
+                const int2 v = *reinterpret_cast<const int2 *>(A + (size_t)y * lda + k0 + ak);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    la[i] = (float)(int8_t)(((i < 4 ? v.x : v.y) >> (8 * (i & 3))) & 0xff);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) la[i] = (float)A[(size_t)y * lda + k0 + ak + i];
+            }
+            const float *Bk = B + (size_t)(k0 + bk) * ldb + n0 + bc;
+            if (vecB) {
+                const float4 b0 = *reinterpret_cast<const float4 *>(Bk);
+                const float4 b1 = *reinterpret_cast<const float4 *>(Bk + 32);
+                lb[0] = b0.x, lb[1] = b0.y, lb[2] = b0.z, lb[3] = b0.w;
+                lb[4] = b1.x, lb[5] = b1.y, lb[6] = b1.z, lb[7] = b1.w;
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) lb[4 * h + i] = Bk[32 * h + i];
+            }
+            return;
+        }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int k = k0 + ak + i;
