@@ -40,6 +40,23 @@ public:
     static constexpr size_t kBipLargeWork = (size_t)1 << 22;
     enum State { kQueued = 0, kActive = 1, kDone = 2 };
 
+    // device memory of one request, allocated and freed in stream order (no
+    // device-wide synchronisation per request)
+    struct AsyncMem {
+        unsigned char *p = nullptr;
+        void alloc(size_t bytes, cudaStream_t s) {
+            release(s);
+            SQ_CHECK(cudaMallocAsync((void **)&p, bytes, s));
+        }
+        void release(cudaStream_t s) {
+            if (p) cudaFreeAsync(p, s);
+            p = nullptr;
+        }
+        ~AsyncMem() {
+            if (p) cudaFree(p);
+        }
+    };
+
     struct Request {
         int id, kind;  // 0 dense, 1 bipartite
         int N0, N1, m, optimize, nSteps;
@@ -47,7 +64,9 @@ public:
         std::vector<float> W, b0, b1, G, beta;
         int state = kQueued;
         // resident state
-        DevBuf<unsigned char> mem;
+        AsyncMem mem;
+        double *dE = nullptr;          // FP64 energies, computed when the last step is queued
+        cudaEvent_t done = nullptr;    // recorded after them
         size_t bytes = 0;
         int pos = 0;     // steps done
         int slot = -1;   // batch slot, -1 for the per-instance kernel
@@ -77,7 +96,19 @@ public:
         stageSmem_ = std::min(sq103_dense_batch_max_smem(), 96 * 1024);
         denseGrid_ = sms_ * std::max(1, sq103_dense_batch_ctas_per_sm(stageSmem_));
         bipGrid_ = sms_ * 4;
+        // request memory comes from the device's stream-ordered pool: keep what is
+        // freed for the next requests instead of returning it at every sync
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
         st_.sync();
+    }
+
+    ~Server() {
+        for (Request *r : finishing_)
+            if (r->done) cudaEventDestroy(r->done);
     }
 
     int submitDense(const float *W, int N, int m, int optimize, unsigned long long seed, const float *G,
@@ -110,6 +141,7 @@ public:
     // kStepsPerTick steps (one refresh period) of every active instance; returns the
     // number of requests completed
     int tick() {
+        const int nDone = finalizeReady(false);
         admit();
         const int nD = (int)denseSlots_.size(), nB = (int)bipSlots_.size();
         if (nD > 0)
@@ -141,14 +173,18 @@ public:
         std::vector<Request *> finished;
         for (auto &kv : active_) {
             Request *r = kv.second;
+            if (r->pos >= r->nSteps) continue;  // finishing: its results are being collected
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)
                 SQ_CHECK(sq103_dense_field_refresh(r->dt.J, r->dt.ldJ, r->dt.q, r->dt.F, r->N0, r->m, st_.get()));
             if (r->pos >= r->nSteps) finished.push_back(r);
         }
-        for (Request *r : finished) complete(r);
+        for (Request *r : finished) finish(r);
         ++ticks_;
-        return (int)finished.size();
+        // nothing left to step (queued requests wait for memory or slots that only
+        // collected results free): wait for the results still being computed
+        if (active_.size() == finishing_.size()) return nDone + finalizeReady(true);
+        return nDone;
     }
 
     int state(int id) const {
@@ -269,9 +305,11 @@ private:
             const size_t N = r->N0;
             const size_t ldJ = ldj(N);  // rows padded to 16 bytes for the one-CTA-per-trotter sweep
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * ldJ * 4), oc = oh + al(N * 4),
-                   oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), tot = oR + al(m * N * 8);
-            r->mem.ensure(tot);
+                   oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), oE = oR + al(m * N * 8),
+                   tot = oE + al(m * 8);
+            r->mem.alloc(tot, st_.get());
             unsigned char *b = r->mem.p;
+            r->dE = (double *)(b + oE);
             float *G = (float *)(b + oG), *beta = (float *)(b + oB), *J = (float *)(b + oJ), *h = (float *)(b + oh);
             float *c32 = (float *)(b + oc);
             r->c64 = (double *)(b + oc + 256);
@@ -308,9 +346,11 @@ private:
             const size_t N0 = r->N0, N1 = r->N1;
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh0 = oJ + al(N0 * N1 * 4), oh1 = oh0 + al(N0 * 4),
                    oc = oh1 + al(N1 * 4), oq0 = oc + 512, oq1 = oq0 + al(m * N0), oF0 = oq1 + al(m * N1),
-                   oF1 = oF0 + al(m * N0 * 4), oR = oF1 + al(m * N1 * 4), tot = oR + al(std::max(m * N1, N0 + N1) * 8);
-            r->mem.ensure(tot);
+                   oF1 = oF0 + al(m * N0 * 4), oR = oF1 + al(m * N1 * 4), oE = oR + al(std::max(m * N1, N0 + N1) * 8),
+                   tot = oE + al(m * 8);
+            r->mem.alloc(tot, st_.get());
             unsigned char *b = r->mem.p;
+            r->dE = (double *)(b + oE);
             float *G = (float *)(b + oG), *beta = (float *)(b + oB), *J = (float *)(b + oJ);
             float *h0 = (float *)(b + oh0), *h1 = (float *)(b + oh1), *c32 = (float *)(b + oc);
             r->c64 = (double *)(b + oc + 256);
@@ -351,45 +391,73 @@ private:
     }
 
     // FP64 energies and spins out, memory and slot released
-    void complete(Request *r) {
+    // The request has queued its last step: its FP64 energies are queued behind
+    // it and collected by finalizeReady() once an event says they are done, so
+    // the host never waits for the GPU here.
+    void finish(Request *r) {
         const int m = r->m;
-        DevBuf<double> E;
-        E.ensure(m);
-        r->E.resize(m);
         if (r->kind == 0) {
             const int N = r->N0;
             double *scratch = (double *)((unsigned char *)r->dt.q + al((size_t)m * N));
-            SQ_CHECK(sq103_dense_energy(r->dt.J, r->dt.ldJ, r->dt.h, r->c64, r->dt.q, N, m, r->optimize, scratch, E.p,
-                                        nullptr,
-                                        st_.get()));
-            r->q0.resize((size_t)m * N);
-            SQ_CHECK(cudaMemcpyAsync(r->q0.data(), r->dt.q, (size_t)m * N, cudaMemcpyDeviceToHost, st_.get()));
+            SQ_CHECK(sq103_dense_energy(r->dt.J, r->dt.ldJ, r->dt.h, r->c64, r->dt.q, N, m, r->optimize, scratch,
+                                        r->dE, nullptr, st_.get()));
         } else {
-            const int N0 = r->N0, N1 = r->N1;
-            double *scratch = (double *)((unsigned char *)r->bt.F1 + al((size_t)m * N1 * 4));
-            SQ_CHECK(sq103_bipartite_energy(r->bt.J, r->bt.h0, r->bt.h1, r->c64, r->bt.q0, r->bt.q1, N0, N1, m,
-                                            r->optimize, scratch, E.p, nullptr, st_.get()));
-            r->q0.resize((size_t)m * N0);
-            r->q1.resize((size_t)m * N1);
-            SQ_CHECK(cudaMemcpyAsync(r->q0.data(), r->bt.q0, (size_t)m * N0, cudaMemcpyDeviceToHost, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(r->q1.data(), r->bt.q1, (size_t)m * N1, cudaMemcpyDeviceToHost, st_.get()));
+            double *scratch = (double *)((unsigned char *)r->bt.F1 + al((size_t)m * r->N1 * 4));
+            SQ_CHECK(sq103_bipartite_energy(r->bt.J, r->bt.h0, r->bt.h1, r->c64, r->bt.q0, r->bt.q1, r->N0, r->N1,
+                                            m, r->optimize, scratch, r->dE, nullptr, st_.get()));
         }
-        SQ_CHECK(cudaMemcpyAsync(r->E.data(), E.p, sizeof(double) * m, cudaMemcpyDeviceToHost, st_.get()));
-        int status = 0;
-        SQ_CHECK(cudaMemcpyAsync(&status, status_.p, sizeof(int), cudaMemcpyDeviceToHost, st_.get()));
-        st_.sync();
-        throwErrorIf(status != 0, "a dense sweep kernel reported status %d.", status);
-        // free the slot: the last slot moves into it
+        SQ_CHECK(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
+        SQ_CHECK(cudaEventRecord(r->done, st_.get()));
+        // free the slot now (the kernels skip finished instances anyway): the last slot moves into it
         if (r->kind == 0 && !r->large) removeSlot(denseSlots_, r, dTasks_.p, dPos_.p, 0);
         if (r->kind == 1 && !r->large) removeSlot(bipSlots_, r, bTasks_.p, bPos_.p, 1);
         if (r->large) large_.erase(std::find(large_.begin(), large_.end(), r));
-        st_.sync();
-        r->mem.release();
-        used_ -= r->bytes;
-        active_.erase(r->id);
-        r->state = kDone;
-        completed_.push_back(r->id);
-        ++done_;
+        finishing_.push_back(r);
+    }
+
+    // Collects, in completion order, the requests whose energies are done (all
+    // of them when wait): energies, spins and the status word are copied on the
+    // result stream, which waits only for that request's event, and its memory
+    // is released.  Returns how many became done.
+    int finalizeReady(bool wait) {
+        int n = 0;
+        while (!finishing_.empty()) {
+            Request *r = finishing_.front();
+            if (wait) {
+                SQ_CHECK(cudaEventSynchronize(r->done));
+            } else {
+                const cudaError_t q = cudaEventQuery(r->done);
+                if (q == cudaErrorNotReady) break;
+                SQ_CHECK(q);
+            }
+            finishing_.pop_front();
+            const int m = r->m;
+            cudaStream_t rs = res_.get();
+            SQ_CHECK(cudaStreamWaitEvent(rs, r->done, 0));
+            r->E.resize(m);
+            SQ_CHECK(cudaMemcpyAsync(r->E.data(), r->dE, sizeof(double) * m, cudaMemcpyDeviceToHost, rs));
+            const int8_t *dq0 = r->kind == 0 ? r->dt.q : r->bt.q0;
+            r->q0.resize((size_t)m * r->N0);
+            SQ_CHECK(cudaMemcpyAsync(r->q0.data(), dq0, r->q0.size(), cudaMemcpyDeviceToHost, rs));
+            if (r->kind == 1) {
+                r->q1.resize((size_t)m * r->N1);
+                SQ_CHECK(cudaMemcpyAsync(r->q1.data(), r->bt.q1, r->q1.size(), cudaMemcpyDeviceToHost, rs));
+            }
+            int status = 0;
+            SQ_CHECK(cudaMemcpyAsync(&status, status_.p, sizeof(int), cudaMemcpyDeviceToHost, rs));
+            SQ_CHECK(cudaStreamSynchronize(rs));
+            cudaEventDestroy(r->done);
+            r->done = nullptr;
+            r->mem.release(st_.get());
+            used_ -= r->bytes;
+            active_.erase(r->id);
+            r->state = kDone;
+            completed_.push_back(r->id);
+            ++done_;
+            ++n;
+            throwErrorIf(status != 0, "a dense sweep kernel reported status %d.", status);
+        }
+        return n;
     }
 
     template <class T>
@@ -409,7 +477,7 @@ private:
         SQ_CHECK(cudaMemcpyAsync(counts_.p + which, &hostCount_[which], sizeof(int), cudaMemcpyHostToDevice, st_.get()));
     }
 
-    Stream st_;
+    Stream st_, res_;  // work; result copies
     unsigned long long budget_, used_ = 0;
     int maxSlots_, maxLarge_ = 4, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
     long long ticks_ = 0;
@@ -419,6 +487,7 @@ private:
     std::deque<int> completed_;
     std::map<int, Request *> active_;
     std::vector<Request *> denseSlots_, bipSlots_, large_;
+    std::deque<Request *> finishing_;  // last step queued, results not yet collected
     DevBuf<sq103_dense_task> dTasks_;
     DevBuf<sq103_bipartite_task> bTasks_;
     DevBuf<int> dPos_, bPos_, counts_, queues_, status_;
