@@ -325,6 +325,7 @@ def run_served(args, world):
     srv.set_large_limit(args.large)
     ticks = 0
     ids, arrival, finish = {}, {}, {}
+    t_gen = t_submit = t_tick = 0.0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     k = 0
@@ -333,14 +334,20 @@ def run_served(args, world):
         if now >= T:
             break
         while k < len(reqs) and reqs[k]["t"] <= now:
+            ta = time.perf_counter()
             r, d = reqs[k], _couplings(reqs[k])
+            tb = time.perf_counter()
             if r["dense"]:
                 rid = srv.submit_dense(d, r["m"], G, BETA, sq.minimize, seed=r["seed"])
             else:
                 rid = srv.submit_bipartite(d[0], d[1], d[2], r["m"], G, BETA, sq.minimize, seed=r["seed"])
+            t_gen += tb - ta
+            t_submit += time.perf_counter() - tb
             ids[rid], arrival[rid] = k, r["t"]
             k += 1
+        tc = time.perf_counter()
         nc = srv.tick()
+        t_tick += time.perf_counter() - tc
         ticks += 1
         if nc:
             t_now = time.perf_counter() - t0
@@ -352,6 +359,7 @@ def run_served(args, world):
     lat = sorted(finish[r] - arrival[r] for r in finish)
     served = {"solves": len(finish), "window_s": T, "solves_per_s": len(finish) / T, "submitted": k,
               "ticks": ticks, "ms_per_tick": 1000.0 * T / max(ticks, 1),
+              "host_s": {"generate_couplings": t_gen, "submit": t_submit, "tick": t_tick},
               "p50_s": lat[len(lat) // 2] if lat else None,
               "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None}
     del srv
@@ -738,7 +746,8 @@ def main():
                          "bipartite: N0=N1=1024 m=64 sweep; bf: dense brute force N=32")
     ap.add_argument("--window", type=float, default=20.0, help="served mode: seconds per path")
     ap.add_argument("--slots", type=int, default=512, help="served mode: concurrent instances per kind")
-    ap.add_argument("--large", type=int, default=4, help="served mode: concurrent whole-GPU instances")
+    ap.add_argument("--large", type=int, default=8,
+                    help="served mode: concurrent large instances (dense ones step together in packed launches)")
     ap.add_argument("--check", type=int, default=16, help="served mode: requests compared with the plain path")
     ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")
     ap.add_argument("--plain-sample", type=int, default=16, help="batched mode: instances solved on the plain path")

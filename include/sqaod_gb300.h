@@ -91,6 +91,13 @@ SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps);
 /* 1 if the one-CTA-per-trotter sweep can run this shape on the current device (N >= 64, m >= 2;
  * the launch also needs ldJ % 4 == 0 and a 16-byte aligned J) */
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
+/* No counterpart in the reference.  Up to 8 independent instances in one
+ * cooperative launch of the one-CTA-per-trotter sweep (their trotter counts
+ * summed within sq103_dense_multicta_capacity of the largest N); each task
+ * needs its own ws.  Every instance ends exactly as when launched alone. */
+SQ103_API int sq103_dense_anneal_pack(const sq103_dense_task *tasks, int n, void *stream);
+/* CTAs of the one-CTA-per-trotter sweep that can be resident at once for rows of N spins */
+SQ103_API int sq103_dense_multicta_capacity(int N);
 
 /* QUBO -> Ising (h, J, c); replaces DeviceDenseGraphFormulas::calculateHamiltonian
  * (sqaodc/cuda/DeviceFormulas.cpp:24-31).  scratch: N doubles. */
@@ -375,9 +382,8 @@ SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int
                                   long long capBytes, int release);
 SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *done,
                                  unsigned long long *bytesInUse);
-/* at most n instances on the whole-GPU paths at a time (default 4; dense: one CTA per
- * trotter, bipartite: per-instance kernels): each
- * of them steps with the whole GPU every tick */
+/* at most n large instances admitted at a time (default 8; dense: one CTA per
+ * trotter, packed up to 8 per launch; bipartite: per-instance kernels) */
 SQ103_API int sq103_server_set_large_limit(void *handle, int n);
 /* ids of the requests completed since the last call (at most cap, in completion order) */
 SQ103_API int sq103_server_completed(void *handle, int *ids, int cap, int *n);

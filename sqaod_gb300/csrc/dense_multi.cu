@@ -46,6 +46,8 @@
 // strictly earlier trials and cannot form a cycle.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 
@@ -188,11 +190,50 @@ __device__ __forceinline__ void window_bits(int x, int Ji, int j0, int pLast, in
     }
 }
 
-__global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(sq103_dense_task T, unsigned long long *outLog,
-                                                                   int nWords) {
+// Up to kMaxPack independent instances in one cooperative launch: CTAs
+// [base[i], base[i+1]) are the trotters of task t[i], whose accept words live in
+// outLog[i] (nWords[i] per trotter).  Instances do not interact (the prologue's
+// grid sync is the only common step), so each runs exactly as alone.
+constexpr int kMaxPack = 8;
+struct McPack {
+    sq103_dense_task t[kMaxPack];
+    unsigned long long *outLog[kMaxPack];
+    int nWords[kMaxPack];
+    int base[kMaxPack + 1];
+    int n;
+};
+
+__global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ McShared S;
-    const int y = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    __shared__ sq103_dense_task task;
+    __shared__ unsigned long long *sLog;
+    __shared__ int sWords, sBase;
+    if (threadIdx.x == 0) {
+        int ti = 0;
+#pragma unroll
+        for (int i = 1; i < kMaxPack; ++i)
+            if (i < P.n && (int)blockIdx.x >= P.base[i]) ti = i;
+        // constant indices only (a runtime index into the parameters would copy them all)
+        switch (ti) {
+#define SQ103_PICK(i)            \
+    case i:                      \
+        task = P.t[i];           \
+        sLog = P.outLog[i];      \
+        sWords = P.nWords[i];    \
+        sBase = P.base[i];       \
+        break;
+            SQ103_PICK(0) SQ103_PICK(1) SQ103_PICK(2) SQ103_PICK(3)
+            SQ103_PICK(4) SQ103_PICK(5) SQ103_PICK(6) SQ103_PICK(7)
+#undef SQ103_PICK
+        }
+    }
+    __syncthreads();
+    static_assert(kMaxPack == 8, "one case per pack entry");
+    const sq103_dense_task &T = task;
+    unsigned long long *const outLog = sLog;
+    const int nWords = sWords;
+    const int y = (int)blockIdx.x - sBase, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = T.N, m = T.m;
     const bool sa = T.algo == kSANaive;
     const int nNbr = sa ? 0 : (m == 2 ? 1 : 2);
@@ -835,25 +876,50 @@ SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo) {
     return m <= multi_capacity(N) ? 1 : 0;
 }
 
-// launched from sq103_dense_anneal (dense.cu) when the shape and workspace allow it
-int sq103_dense_anneal_multi(const sq103_dense_task *t, void *stream) {
+// n instances in one cooperative launch (see McPack)
+static int launch_pack(const sq103_dense_task *tasks, int n, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
-    const int N = t->N, m = t->m;
-    if ((long long)t->nSteps * N >= (1ll << 31)) return kErrBadShape;
-    // rows of J are read as float4
-    if ((t->ldJ & 3) || (reinterpret_cast<uintptr_t>(t->J) & 15)) return kErrBadShape;
-    if (!t->ws || t->wsBytes < sq103_dense_ws_bytes(N, m, t->nSteps)) return kErrCapacity;
-    if (multi_capacity(N) < m) return kErrCapacity;
-    unsigned long long *outLog = reinterpret_cast<unsigned long long *>(t->ws);
-    int nWords = (int)(((long long)t->nSteps * N + 31) / 32);
-    // the accept words carry their batch tag; zero means "not published"
-    cudaError_t e = cudaMemsetAsync(outLog, 0, (size_t)m * nWords * 8, st);
-    if (e != cudaSuccess) return (int)e;
-    sq103_dense_task task = *t;
-    void *args[] = {&task, &outLog, &nWords};
-    e = cudaLaunchCooperativeKernel((const void *)dense_sweep_multi, dim3(m), dim3(kMcThreads), args,
-                                    multi_smem_bytes(N), st);
-    return (int)e;
+    if (n < 1 || n > kMaxPack) return kErrBadShape;
+    McPack P = {};
+    P.n = n;
+    int maxN = 0, ctas = 0;
+    for (int i = 0; i < n; ++i) {
+        const sq103_dense_task &t = tasks[i];
+        const int N = t.N, m = t.m;
+        if (t.algo != kColoring && t.algo != kSANaive) return kErrBadShape;
+        if (N < 64 || m < 2 || t.nSteps < 1) return kErrBadShape;
+        if ((long long)t.nSteps * N >= (1ll << 31)) return kErrBadShape;
+        // rows of J are read as float4
+        if ((t.ldJ & 3) || (reinterpret_cast<uintptr_t>(t.J) & 15)) return kErrBadShape;
+        if (!t.ws || t.wsBytes < sq103_dense_ws_bytes(N, m, t.nSteps)) return kErrCapacity;
+        P.t[i] = t;
+        P.outLog[i] = reinterpret_cast<unsigned long long *>(t.ws);
+        P.nWords[i] = (int)(((long long)t.nSteps * N + 31) / 32);
+        P.base[i] = ctas;
+        ctas += m;
+        maxN = std::max(maxN, N);
+    }
+    for (int i = n; i <= kMaxPack; ++i) P.base[i] = ctas;
+    // every CTA resident at once (cooperative launch); also sets the kernel's shared-memory limit
+    if (multi_capacity(maxN) < ctas) return kErrCapacity;
+    for (int i = 0; i < n; ++i) {
+        // the accept words carry their batch tag; zero means "not published"
+        cudaError_t e = cudaMemsetAsync(P.outLog[i], 0, (size_t)tasks[i].m * P.nWords[i] * 8, st);
+        if (e != cudaSuccess) return (int)e;
+    }
+    void *args[] = {&P};
+    return (int)cudaLaunchCooperativeKernel((const void *)dense_sweep_multi, dim3(ctas), dim3(kMcThreads), args,
+                                           multi_smem_bytes(maxN), st);
 }
+
+// launched from sq103_dense_anneal (dense.cu) when the shape and workspace allow it
+int sq103_dense_anneal_multi(const sq103_dense_task *t, void *stream) { return launch_pack(t, 1, stream); }
+
+SQ103_API int sq103_dense_anneal_pack(const sq103_dense_task *tasks, int n, void *stream) {
+    if (!tasks) return kErrBadShape;
+    return launch_pack(tasks, n, stream);
+}
+
+SQ103_API int sq103_dense_multicta_capacity(int N) { return N >= 64 ? multi_capacity(N) : 0; }
 
 }  // extern "C"

@@ -150,25 +150,40 @@ public:
         if (nB > 0)
             SQ_CHECK(sq103_bipartite_batch_launch(bTasks_.p, nB, counts_.p + 1, nullptr, bPos_.p, queues_.p + 2,
                                                   kStepsPerTick, std::min(bipGrid_, nB), st_.get()));
+        // large dense instances: packed cooperative launches (instances of similar
+        // size together, as many trotters as can be resident); large bipartite: one by one
+        std::vector<Request *> big;
+        for (Request *r : large_)
+            if (r->kind == 0) big.push_back(r);
+        std::sort(big.begin(), big.end(), [](const Request *a, const Request *b) { return a->N0 < b->N0; });
+        std::vector<sq103_dense_task> pack;
+        int packM = 0, packN = 0;
+        auto flush = [&]() {
+            if (!pack.empty()) SQ_CHECK(sq103_dense_anneal_pack(pack.data(), (int)pack.size(), st_.get()));
+            pack.clear();
+            packM = packN = 0;
+        };
+        for (Request *r : big) {
+            sq103_dense_task t = r->dt;
+            t.G = r->dt.G + r->pos;
+            t.beta = r->dt.beta + r->pos;
+            t.step0 = 1 + (uint32_t)r->pos;
+            t.nSteps = std::min(kStepsPerTick, r->nSteps - r->pos);
+            const int N2 = std::max(packN, r->N0);
+            if (pack.size() == (size_t)kMaxPack || packM + r->m > sq103_dense_multicta_capacity(N2)) flush();
+            pack.push_back(t);
+            packM += r->m;
+            packN = std::max(packN, r->N0);
+        }
+        flush();
         for (Request *r : large_) {
-            const int n = std::min(kStepsPerTick, r->nSteps - r->pos);
-            if (r->kind == 0) {
-                sq103_dense_task t = r->dt;
-                t.G = r->dt.G + r->pos;
-                t.beta = r->dt.beta + r->pos;
-                t.step0 = 1 + (uint32_t)r->pos;
-                t.nSteps = n;
-                t.ws = ws_.p;
-                t.wsBytes = ws_.n;
-                SQ_CHECK(sq103_dense_anneal(&t, st_.get()));
-            } else {
-                sq103_bipartite_task t = r->bt;
-                t.G = r->bt.G + r->pos;
-                t.beta = r->bt.beta + r->pos;
-                t.step0 = 1 + (uint32_t)r->pos;
-                t.nSteps = n;
-                SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
-            }
+            if (r->kind != 1) continue;
+            sq103_bipartite_task t = r->bt;
+            t.G = r->bt.G + r->pos;
+            t.beta = r->bt.beta + r->pos;
+            t.step0 = 1 + (uint32_t)r->pos;
+            t.nSteps = std::min(kStepsPerTick, r->nSteps - r->pos);
+            SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
         }
         std::vector<Request *> finished;
         for (auto &kv : active_) {
@@ -306,7 +321,9 @@ private:
             const size_t ldJ = ldj(N);  // rows padded to 16 bytes for the one-CTA-per-trotter sweep
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * ldJ * 4), oc = oh + al(N * 4),
                    oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), oE = oR + al(m * N * 8),
-                   tot = oE + al(m * 8);
+                   oWs = oE + al(m * 8),
+                   tot = oWs + (r->large ? al(sq103_dense_ws_bytes((int)N, m, kStepsPerTick)) : 0);
+            r->bytes += tot - oWs;  // the accept-word workspace of a large instance
             r->mem.alloc(tot, st_.get());
             unsigned char *b = r->mem.p;
             r->dE = (double *)(b + oE);
@@ -333,7 +350,8 @@ private:
             t.nSteps = n;
             t.status = status_.p;
             if (r->large) {
-                ws_.ensure(std::max<unsigned long long>(ws_.n, sq103_dense_ws_bytes((int)N, m, kStepsPerTick)));
+                t.ws = b + oWs;  // its own: large instances step together in packed launches
+                t.wsBytes = sq103_dense_ws_bytes((int)N, m, kStepsPerTick);
                 large_.push_back(r);
             } else {
                 r->slot = (int)denseSlots_.size();
@@ -479,7 +497,7 @@ private:
 
     Stream st_, res_;  // work; result copies
     unsigned long long budget_, used_ = 0;
-    int maxSlots_, maxLarge_ = 4, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
+    int maxSlots_, maxLarge_ = 8, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
     long long ticks_ = 0;
     int hostCount_[2] = {0, 0};
     std::map<int, std::unique_ptr<Request>> all_;
@@ -492,7 +510,7 @@ private:
     DevBuf<sq103_bipartite_task> bTasks_;
     DevBuf<int> dPos_, bPos_, counts_, queues_, status_;
     DevBuf<float> dW_;
-    DevBuf<unsigned char> ws_;
+    static constexpr int kMaxPack = 8;  // instances per packed launch (sq103_dense_anneal_pack)
 };
 
 }  // namespace sq103

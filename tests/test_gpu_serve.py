@@ -95,6 +95,30 @@ def test_server_requests_match_alone():
             assert np.array_equal(q[1], np.array([p[1] for p in q1])), i
 
 
+def test_server_packs_large_dense_requests():
+    """Large dense requests of different sizes and lengths step together in
+    packed cooperative launches; each still ends bit-identical to annealing it alone."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    specs = [("d", 1024, 64, 17, "min"), ("d", 700, 32, 9, "max"), ("d", 1500, 16, 12, "min"),
+             ("d", 257, 128, 20, "min"), ("d", 1024, 40, 8, "min")]
+    rng = np.random.default_rng(23)
+    data = [_sym(rng, sp[1]) for sp in specs]
+    srv = AnnealServer(budget_bytes=1 << 30, max_slots=8)
+    srv.set_large_limit(8)
+    ids = []
+    for i, (spec, d) in enumerate(zip(specs, data)):
+        G, beta = _schedule(spec[3])
+        ids.append(srv.submit_dense(d, spec[2], G, beta, sq.maximize if spec[4] == "max" else sq.minimize,
+                                    seed=2000 + i))
+    assert srv.run(max_ticks=100) < 100
+    for i, (spec, d, rid) in enumerate(zip(specs, data, ids)):
+        E, q = srv.result(rid)
+        E1, q1 = _alone(sq, spec, d, 2000 + i)
+        assert np.array_equal(E, E1), (i, E, E1)
+        assert np.array_equal(q, np.array(q1)), i
+
+
 def test_server_rejects_oversized_request():
     import sqaod_gb300 as sq
     from sqaod_gb300._lib import SqaodError
