@@ -18,9 +18,11 @@ def _schedule(n):
 def _problems(k, seed=0):
     rng = np.random.default_rng(seed)
     out = []
-    for i in range(k):
-        N = int(rng.choice([40, 64, 96, 130, 200, 256]))
-        m = int(rng.choice([1, 2, 8, 16, 32]))
+    # small instances (one CTA each in the persistent launch) and, last, instances
+    # too large to stage (packed one-CTA-per-trotter launches; N = 1030 pads its rows)
+    shapes = [(int(rng.choice([40, 64, 96, 130, 200, 256])), int(rng.choice([1, 2, 8, 16, 32]))) for _ in range(k)]
+    shapes += [(600, 24), (1030, 16), (300, 64)]
+    for i, (N, m) in enumerate(shapes):
         W = rng.uniform(-1, 1, (N, N))
         W = (np.triu(W) + np.triu(W, 1).T).astype(np.float32)
         out.append((W, m, 100 + i))
