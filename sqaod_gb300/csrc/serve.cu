@@ -18,6 +18,7 @@
 // slot and memory are released in the same tick, so a waiting request can be
 // admitted by the next tick.  No counterpart in the reference.
 #include <algorithm>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
@@ -57,6 +58,47 @@ public:
         }
     };
 
+    // Pinned staging for every host-to-device copy of the server: from pageable
+    // memory cudaMemcpyAsync may wait for the stream, stalling the host behind
+    // every queued tick.  Two halves are used in turn; a half is reused only
+    // after an event recorded when it was left has passed.
+    struct PinnedStage {
+        unsigned char *base = nullptr;
+        size_t half = 0, off = 0;
+        int cur = 0;
+        cudaEvent_t left[2] = {nullptr, nullptr};
+        bool pending[2] = {false, false};
+        ~PinnedStage() {
+            if (base) cudaFreeHost(base);
+            for (cudaEvent_t e : left)
+                if (e) cudaEventDestroy(e);
+        }
+        void init(size_t halfBytes) {
+            SQ_CHECK(cudaMallocHost((void **)&base, 2 * halfBytes));
+            half = halfBytes;
+            for (cudaEvent_t &e : left) SQ_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        void copy(void *dst, const void *src, size_t n, cudaStream_t s) {
+            if (n > half) {  // larger than a half: directly from the caller's memory
+                SQ_CHECK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s));
+                return;
+            }
+            const size_t need = (n + 255) & ~(size_t)255;
+            if (off + need > half) {
+                SQ_CHECK(cudaEventRecord(left[cur], s));
+                pending[cur] = true;
+                cur ^= 1;
+                if (pending[cur]) SQ_CHECK(cudaEventSynchronize(left[cur]));
+                pending[cur] = false;
+                off = 0;
+            }
+            unsigned char *p = base + cur * half + off;
+            memcpy(p, src, n);
+            off += need;
+            SQ_CHECK(cudaMemcpyAsync(dst, p, n, cudaMemcpyHostToDevice, s));
+        }
+    };
+
     struct Request {
         int id, kind;  // 0 dense, 1 bipartite
         int N0, N1, m, optimize, nSteps;
@@ -87,6 +129,7 @@ public:
         counts_.ensure(2);
         queues_.ensure(4);
         status_.ensure(1);
+        stage_.init((size_t)96 << 20);
         SQ_CHECK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_.get()));
         SQ_CHECK(cudaMemsetAsync(queues_.p, 0, sizeof(int) * 4, st_.get()));
         SQ_CHECK(cudaMemsetAsync(counts_.p, 0, sizeof(int) * 2, st_.get()));
@@ -309,8 +352,8 @@ private:
         }
         if (changed) {
             int c[2] = {(int)denseSlots_.size(), (int)bipSlots_.size()};
-            // (pageable source: staged before the call returns)
-            SQ_CHECK(cudaMemcpyAsync(counts_.p, c, sizeof(c), cudaMemcpyHostToDevice, st_.get()));
+            // (through the pinned stage: the host does not wait for the stream)
+            stage_.copy(counts_.p, c, sizeof(c), st_.get());
         }
     }
 
@@ -333,10 +376,10 @@ private:
             float *F = (float *)(b + oF);
             int8_t *q = (int8_t *)(b + oq);
             double *scratch = (double *)(b + oR);  // N doubles for the hamiltonian, m N for energies
-            SQ_CHECK(cudaMemcpyAsync(G, r->G.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(beta, r->beta.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            stage_.copy(G, r->G.data(), 4 * n, st_.get());
+            stage_.copy(beta, r->beta.data(), 4 * n, st_.get());
             dW_.ensure(N * N);
-            SQ_CHECK(cudaMemcpyAsync(dW_.p, r->W.data(), 4 * N * N, cudaMemcpyHostToDevice, st_.get()));
+            stage_.copy(dW_.p, r->W.data(), 4 * N * N, st_.get());
             SQ_CHECK(cudaMemsetAsync(J, 0, sizeof(float) * N * ldJ, st_.get()));
             SQ_CHECK(sq103_dense_hamiltonian(dW_.p, (int)N, (int)N, r->optimize, h, J, (int)ldJ, c32, r->c64, scratch,
                                              st_.get()));
@@ -357,8 +400,8 @@ private:
                 r->slot = (int)denseSlots_.size();
                 denseSlots_.push_back(r);
                 int zero = 0;
-                SQ_CHECK(cudaMemcpyAsync(dTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
-                SQ_CHECK(cudaMemcpyAsync(dPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+                stage_.copy(dTasks_.p + r->slot, &t, sizeof(t), st_.get());
+                stage_.copy(dPos_.p + r->slot, &zero, sizeof(int), st_.get());
             }
         } else {
             const size_t N0 = r->N0, N1 = r->N1;
@@ -375,12 +418,12 @@ private:
             int8_t *q0 = (int8_t *)(b + oq0), *q1 = (int8_t *)(b + oq1);
             float *F0 = (float *)(b + oF0), *F1 = (float *)(b + oF1);
             double *scratch = (double *)(b + oR);
-            SQ_CHECK(cudaMemcpyAsync(G, r->G.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(beta, r->beta.data(), 4 * n, cudaMemcpyHostToDevice, st_.get()));
+            stage_.copy(G, r->G.data(), 4 * n, st_.get());
+            stage_.copy(beta, r->beta.data(), 4 * n, st_.get());
             dW_.ensure(N0 * N1 + N0 + N1);
-            SQ_CHECK(cudaMemcpyAsync(dW_.p, r->W.data(), 4 * N0 * N1, cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(dW_.p + N0 * N1, r->b0.data(), 4 * N0, cudaMemcpyHostToDevice, st_.get()));
-            SQ_CHECK(cudaMemcpyAsync(dW_.p + N0 * N1 + N0, r->b1.data(), 4 * N1, cudaMemcpyHostToDevice, st_.get()));
+            stage_.copy(dW_.p, r->W.data(), 4 * N0 * N1, st_.get());
+            stage_.copy(dW_.p + N0 * N1, r->b0.data(), 4 * N0, st_.get());
+            stage_.copy(dW_.p + N0 * N1 + N0, r->b1.data(), 4 * N1, st_.get());
             SQ_CHECK(sq103_bipartite_hamiltonian(dW_.p + N0 * N1, dW_.p + N0 * N1 + N0, dW_.p, (int)N0, (int)N1,
                                                  r->optimize, h0, h1, J, c32, r->c64, scratch, st_.get()));
             SQ_CHECK(sq103_randomize_spins(q0, (int)N0, m, r->seed, 0, 0, st_.get()));
@@ -398,8 +441,8 @@ private:
                 r->slot = (int)bipSlots_.size();
                 bipSlots_.push_back(r);
                 int zero = 0;
-                SQ_CHECK(cudaMemcpyAsync(bTasks_.p + r->slot, &t, sizeof(t), cudaMemcpyHostToDevice, st_.get()));
-                SQ_CHECK(cudaMemcpyAsync(bPos_.p + r->slot, &zero, sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+                stage_.copy(bTasks_.p + r->slot, &t, sizeof(t), st_.get());
+                stage_.copy(bPos_.p + r->slot, &zero, sizeof(int), st_.get());
             }
         }
         // copies from pageable host memory return once the data is staged, so
@@ -492,10 +535,11 @@ private:
         r->slot = -1;
         int c = (int)slots.size();
         hostCount_[which] = c;
-        SQ_CHECK(cudaMemcpyAsync(counts_.p + which, &hostCount_[which], sizeof(int), cudaMemcpyHostToDevice, st_.get()));
+        stage_.copy(counts_.p + which, &hostCount_[which], sizeof(int), st_.get());
     }
 
     Stream st_, res_;  // work; result copies
+    PinnedStage stage_;
     unsigned long long budget_, used_ = 0;
     int maxSlots_, maxLarge_ = 8, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
     long long ticks_ = 0;
