@@ -73,15 +73,18 @@ __device__ void bf_block_setup(const float *W, int N, int L, uint64_t hi, float 
             if ((hi >> c) & 1ull) s += (double)W[(size_t)(H - 1 - c) * N + (N - 1 - tid)];
         C[tid] = (float)(2. * s);
     }
-    if (tid == 32) {
+    if (tid >= 32 && tid < 64) {
+        // E_hh(hi): the second warp sums the selected rows (one per lane, FP64) and
+        // reduces them in a fixed tree order
         double e = 0.;
-        for (int c = 0; c < H; ++c) {
+        for (int c = tid - 32; c < H; c += 32) {
             if (!((hi >> c) & 1ull)) continue;
             const float *row = W + (size_t)(H - 1 - c) * N;
             for (int d = 0; d < H; ++d)
                 if ((hi >> d) & 1ull) e += (double)row[H - 1 - d];
         }
-        *base = (float)e;
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+        if (tid == 32) *base = (float)e;
     }
     __syncthreads();
     // tables over the two halves of lo: lo = (a << Ll) | b
