@@ -70,6 +70,9 @@ constexpr int kCand = 2;        // neighbour iterations per lane and batch found
 constexpr int kPredRows = 8;    // predicted accepting lanes whose gathers are kept in registers
 constexpr float kFieldDrift = 1.f;  // assumed field change between prefetch and decision
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;
+// the prefetchers run ahead and mostly wait: they poll gently, which leaves the
+// SM's shared load/store path to the decider
+constexpr int kPrefetchSleepNs = 128;
 constexpr unsigned FULL = 0xffffffffu;
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
@@ -139,13 +142,13 @@ __device__ __forceinline__ unsigned long long uniform_acquire64(const volatile u
 __device__ __forceinline__ int avail_of(unsigned long long v, int n) { return (int)(n ? v >> 32 : v & 0xffffffffu); }
 
 // bounded wait on a warp-uniform condition; false on timeout
-template <class F>
+template <int SLEEP_NS = 32, class F>
 __device__ __forceinline__ bool wait_until(F &&ready) {
     unsigned long long t0 = 0;
     while (!ready()) {
         if (t0 == 0) t0 = global_ns();
         if (global_ns() - t0 > kWaitLimitNs) return false;
-        __nanosleep(32);
+        __nanosleep(SLEEP_NS);
     }
     return true;
 }
@@ -608,7 +611,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             // and ring slots j - kRing are applied for the neighbours' iterations j of batch p
             const int jEnd = 32 * p + 32;
             int stop = 0;
-            if (!wait_until([&] {
+            if (!wait_until<kPrefetchSleepNs>([&] {
                     int ok = 0;
                     if (lane == 0) {
                         stop = S.done;
@@ -689,7 +692,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 }
                 // batch p - 1 (the other prefetcher's) must be in the ring; its buffer
                 // slot may already hold a later batch (batch p - 2 is this warp's own)
-                if (p > 0 && !wait_until([&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
+                if (p > 0 && !wait_until<kPrefetchSleepNs>([&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
                     break;
                 __syncwarp();
                 const int hb = x & (kBmBits - 1);
