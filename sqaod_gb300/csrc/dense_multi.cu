@@ -16,7 +16,7 @@
 //           trials.  The batch's fields start from the resident row F[y][:],
 //           which the updaters keep one batch behind, plus the previous
 //           batch's flips d_f * J[x_f][x_i], gathered at the batch boundary and
-//           added after the neighbour work of the next batch.
+//           added after the next batch's ghost-row update.
 //           Decisions are published as one 64-bit word per batch (accept
 //           bits, decided count, batch tag) with a single relaxed store after
 //           every accepting round and at the end of the batch: a reader that
@@ -65,7 +65,7 @@ constexpr int kBmWords = kBmBits / 32;
 constexpr int kBmSlots = kRing / 32;  // bitmaps kept per neighbour (one per ring batch)
 constexpr int kPre = 4;         // prefetched batches (power of two)
 constexpr int kJgStride = 32 * 33;
-constexpr int kGv = 16;         // flips of a batch whose gathers are deferred to the next batch
+constexpr int kGv = 8;          // flips of a batch whose gathers are deferred to the next batch
 constexpr int kCand = 2;        // neighbour iterations per lane and batch found by the prefetchers
 constexpr int kPredRows = 8;    // predicted accepting lanes whose gathers are kept in registers
 constexpr float kFieldDrift = 1.f;  // assumed field change between prefetch and decision
@@ -407,15 +407,13 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
 
             // neighbour spins at this batch's sites: apply the published neighbour
             // iterations before this batch's first trial (their sites are in the ring
-            // since this batch's buffer is ready), then correct each lane's site
+            // since this batch's buffer is ready); each lane's site is corrected at the
+            // top of the first round
             qb0 = qb1 = 0;
             nd0 = nd1 = -1;
             unsigned blocked = 0;
-            if (nNbr > 0) {
-                const unsigned long long av = apply_nbr(g0 + before0, g0 + before1);
-                nbr_bits(b, g0, valid, av);
-                blocked = __ballot_sync(FULL, nd0 >= 0 || nd1 >= 0);
-            }
+            unsigned long long avEval = 0;  // availability the lanes' neighbour bits are evaluated with
+            if (nNbr > 0) avEval = apply_nbr(g0 + before0, g0 + before1);
 
             // the previous batch's flips (gathered at the end of that batch)
 #pragma unroll
@@ -427,7 +425,13 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             // decide the batch in rounds
             unsigned pending = __ballot_sync(FULL, valid), accBits = 0;
             float d = 0.f;
+            bool evalNbr = nNbr > 0;  // (one instance of nbr_bits keeps the loop's code small)
             while (pending) {
+                if (evalNbr) {
+                    nbr_bits(b, g0, valid, avEval);
+                    blocked = __ballot_sync(FULL, nd0 >= 0 || nd1 >= 0) & pending;
+                    evalNbr = false;
+                }
                 // a lane with unknown neighbour bits is decided anyway when every value
                 // those bits can take gives the same outcome; it blocks otherwise
                 int acc = 0, amb = 0;
@@ -464,8 +468,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                         break;
                     }
                     // re-evaluate (the ghost rows and A are unchanged within the batch)
-                    nbr_bits(b, g0, valid, av);
-                    blocked = __ballot_sync(FULL, nd0 >= 0 || nd1 >= 0) & pending;
+                    avEval = av;
+                    evalNbr = true;
                     continue;
                 }
                 if (fa == 32) break;  // every undecided lane rejects
