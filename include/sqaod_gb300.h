@@ -355,6 +355,45 @@ SQ103_API int sq103_dense_batch_info(void *handle, int *nInst, int *pos, int *gr
 SQ103_API int sq103_dense_batch_get_E(void *handle, int index, double *E, int cap, int *n);
 SQ103_API int sq103_dense_batch_get_q(void *handle, int index, int8_t *q, int capRows, int *m);
 
+/* ------------------------------------------------ handle layer: formula sets */
+/* The formulas_methods table of the reference's Python extension
+ * (sqaodc/pyglue/formulas.inc:586-605) over the CUDA formula classes
+ * (sqaodc/cuda/CUDAFormulas.cpp:8-294): host buffers in and out, one call
+ * uploads, computes and copies back.  A batch of m = 1 rows is the reference's
+ * single-vector method (dense_graph_calculate_E, ...), m > 1 the batched one.
+ * Energies are FP64 (the reference returns them in the solver's real type);
+ * bits x must be 0 / 1 and spins q -1 / +1, matrices are dense row-major (row
+ * stride = columns) and a dense W or J must be symmetric, or the call fails. */
+SQ103_API int sq103_dg_formulas_new(void **handle);
+SQ103_API int sq103_dg_formulas_delete(void *handle);
+/* E[i] = x_i W x_i^T (dense_graph_calculate_E / dense_graph_batch_calculate_E) */
+SQ103_API int sq103_dg_formulas_calculate_E(void *handle, const float *W, int N, const int8_t *x, int m,
+                                            double *E);
+/* h (N), J (N x N, zero diagonal), c (dense_graph_calculate_hamiltonian) */
+SQ103_API int sq103_dg_formulas_calculate_hamiltonian(void *handle, const float *W, int N, float *h, float *J,
+                                                      float *c);
+/* E[i] = -c - h q_i^T - q_i J q_i^T (dense_graph_[batch_]calculate_E_from_spin) */
+SQ103_API int sq103_dg_formulas_calculate_E_from_spin(void *handle, const float *h, const float *J, float c, int N,
+                                                      const int8_t *q, int m, double *E);
+SQ103_API int sq103_bg_formulas_new(void **handle);
+SQ103_API int sq103_bg_formulas_delete(void *handle);
+/* E[i] = b0 x0_i^T + b1 x1_i^T + x1_i W x0_i^T, W N1 x N0 (bipartite_graph_[batch_]calculate_E) */
+SQ103_API int sq103_bg_formulas_calculate_E(void *handle, const float *b0, const float *b1, const float *W, int N0,
+                                            int N1, const int8_t *x0, const int8_t *x1, int m, double *E);
+/* E[i1 * m0 + i0] = the energy of (x0_i0, x1_i1), m1 x m0 row-major
+ * (bipartite_graph_batch_calculate_E_2d) */
+SQ103_API int sq103_bg_formulas_calculate_E_2d(void *handle, const float *b0, const float *b1, const float *W,
+                                               int N0, int N1, const int8_t *x0, int m0, const int8_t *x1, int m1,
+                                               double *E);
+/* h0 (N0), h1 (N1), J (N1 x N0), c (bipartite_graph_calculate_hamiltonian) */
+SQ103_API int sq103_bg_formulas_calculate_hamiltonian(void *handle, const float *b0, const float *b1,
+                                                      const float *W, int N0, int N1, float *h0, float *h1,
+                                                      float *J, float *c);
+/* E[i] = -c - h0 q0_i^T - h1 q1_i^T - q1_i J q0_i^T (bipartite_graph_[batch_]calculate_E_from_spin) */
+SQ103_API int sq103_bg_formulas_calculate_E_from_spin(void *handle, const float *h0, const float *h1,
+                                                      const float *J, float c, int N0, int N1, const int8_t *q0,
+                                                      const int8_t *q1, int m, double *E);
+
 /* ------------------------------------------- handle layer: request server */
 /* Continuous batching of anneal requests of mixed size and type (no
  * counterpart in the reference).  Requests are admitted in arrival order while

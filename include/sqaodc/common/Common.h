@@ -62,3 +62,5 @@ void log(const char *fmt, ...);
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif
+
+#include <sqaodc/common/Formulas.h>

@@ -1,6 +1,6 @@
 // api.h -- CUDA solver interfaces of the sqaod C++ solver API
 // (sqaodc/cuda/api.h:16-83 of the reference): Device, DeviceAssigner and the
-// CUDA flavours of the four solvers.  Implemented for sm_103a by
+// CUDA flavours of the four solvers and the two formula sets.  Implemented for sm_103a by
 // libsqaod_gb300.so; only <float> is provided.
 #pragma once
 
@@ -49,6 +49,16 @@ struct DenseGraphBFSearcher : DeviceAssigner, sqaod::DenseGraphBFSearcher<real> 
 template <class real>
 struct BipartiteGraphBFSearcher : DeviceAssigner, sqaod::BipartiteGraphBFSearcher<real> {
     virtual ~BipartiteGraphBFSearcher() {}
+};
+
+template <class real>
+struct DenseGraphFormulas : DeviceAssigner, sqaod::DenseGraphFormulas<real> {
+    virtual ~DenseGraphFormulas() {}
+};
+
+template <class real>
+struct BipartiteGraphFormulas : DeviceAssigner, sqaod::BipartiteGraphFormulas<real> {
+    virtual ~BipartiteGraphFormulas() {}
 };
 
 }  // namespace cuda

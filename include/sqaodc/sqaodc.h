@@ -25,6 +25,12 @@ BipartiteGraphBFSearcher<real> *newBipartiteGraphBFSearcher();
 template <class real>
 BipartiteGraphAnnealer<real> *newBipartiteGraphAnnealer();
 
+template <class real>
+DenseGraphFormulas<real> *newDenseGraphFormulas();
+
+template <class real>
+BipartiteGraphFormulas<real> *newBipartiteGraphFormulas();
+
 Device *newDevice(int devNo = -1);
 
 }  // namespace cuda

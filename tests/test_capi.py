@@ -40,6 +40,7 @@ def test_cpp_api_symbols_exported(lib):
     out = subprocess.run(["nm", "-DC", "--defined-only", build.lib_path()], capture_output=True, text=True).stdout
     for sym in ("sqaod::cuda::newDenseGraphAnnealer<float>", "sqaod::cuda::newBipartiteGraphAnnealer<float>",
                 "sqaod::cuda::newDenseGraphBFSearcher<float>", "sqaod::cuda::newBipartiteGraphBFSearcher<float>",
+                "sqaod::cuda::newDenseGraphFormulas<float>", "sqaod::cuda::newBipartiteGraphFormulas<float>",
                 "sqaod::deleteInstance", "sqaod::cuda::newDevice"):
         assert sym in out, sym
 

@@ -1,0 +1,37 @@
+"""Argument rules of sqaod_gb300.cuda.formulas that hold before any device work
+(sqaodpy/sqaod/common/checkers.py, formulas_base.py): no GPU needed."""
+import numpy as np
+import pytest
+
+import sqaod_gb300 as sq
+
+F32 = np.float32
+
+
+def test_float64_is_not_provided():
+    W = np.eye(4)
+    with pytest.raises(RuntimeError, match="float32 only"):
+        sq.cuda.formulas.dense_graph_calculate_E(W, np.zeros(4, np.int8), np.float64)
+    with pytest.raises(RuntimeError, match="float32 only"):
+        sq.cuda.formulas.bipartite_graph_calculate_hamiltonian(np.zeros(2), np.zeros(3), np.zeros((3, 2)),
+                                                              np.float64)
+
+
+def test_shape_and_type_checks():
+    f = sq.cuda.formulas
+    W = np.eye(4, dtype=F32)
+    with pytest.raises(RuntimeError, match="dimension mismatch"):
+        f.dense_graph_calculate_E(W, np.zeros(5, np.int8), F32)
+    with pytest.raises(RuntimeError, match="wrong shape"):
+        f.dense_graph_calculate_hamiltonian(np.zeros((3, 4), F32), F32)
+    with pytest.raises(RuntimeError, match="np.int8"):
+        # the batched spin form takes int8 spins as given, as the reference's does
+        f.dense_graph_batch_calculate_E_from_spin(np.zeros(4, F32), W, 0., np.ones((2, 4), np.int32), F32)
+    with pytest.raises(RuntimeError, match="not a scalar"):
+        f.dense_graph_batch_calculate_E_from_spin(np.zeros(4, F32), W, np.zeros(2), np.ones((2, 4), np.int8), F32)
+    b0, b1, Wb = np.zeros(3, F32), np.zeros(2, F32), np.zeros((2, 3), F32)
+    with pytest.raises(RuntimeError, match="dimension mismatch"):
+        f.bipartite_graph_calculate_E(b0, b1, Wb.T, np.zeros(3, np.int8), np.zeros(2, np.int8), F32)
+    with pytest.raises(RuntimeError, match="dimension mismatch"):
+        f.bipartite_graph_batch_calculate_E_2d(b0, b1, Wb, np.zeros((4, 2), np.int8), np.zeros((4, 2), np.int8),
+                                               F32)
