@@ -259,6 +259,15 @@ SQ103_API int sq103_dg_annealer_anneal(void *handle, const float *G, const float
 SQ103_API int sq103_dg_annealer_get_E64(void *handle, double *E, int cap, int *n);
 SQ103_API int sq103_dg_annealer_get_accepted(void *handle, unsigned long long *accepted);
 SQ103_API int sq103_dg_annealer_get_rng_state(void *handle, unsigned long long *seed, uint32_t *step);
+/* Checkpoint / resume (no counterpart in the reference): q and F are m x N
+ * (spins, resident local fields), sinceRefresh the steps since the last field
+ * refresh.  set_checkpoint needs a prepared annealer of the same problem,
+ * algorithm and trotter count; the run then continues bit for bit as the one
+ * the checkpoint was taken from. */
+SQ103_API int sq103_dg_annealer_get_checkpoint(void *handle, int8_t *q, float *F, unsigned long long *seed,
+                                               uint32_t *step, int *sinceRefresh);
+SQ103_API int sq103_dg_annealer_set_checkpoint(void *handle, const int8_t *q, const float *F, int m, int N,
+                                               unsigned long long seed, uint32_t step, int sinceRefresh);
 SQ103_API int sq103_dg_annealer_set_trace(void *handle, int enable);
 /* kernel selection for the sweep: 0 = automatic, 1 = one CTA per instance, 2 = one CTA per trotter */
 SQ103_API int sq103_dg_annealer_set_kernel(void *handle, int flags);
@@ -292,6 +301,12 @@ SQ103_API int sq103_bg_annealer_anneal(void *handle, const float *G, const float
 SQ103_API int sq103_bg_annealer_get_E64(void *handle, double *E, int cap, int *n);
 SQ103_API int sq103_bg_annealer_get_accepted(void *handle, unsigned long long *accepted);
 SQ103_API int sq103_bg_annealer_get_rng_state(void *handle, unsigned long long *seed, uint32_t *step);
+/* Checkpoint / resume: q0 m x N0, q1 m x N1 spins and the Philox state (the
+ * fields are recomputed from the spins every half step). */
+SQ103_API int sq103_bg_annealer_get_checkpoint(void *handle, int8_t *q0, int8_t *q1, unsigned long long *seed,
+                                               uint32_t *step);
+SQ103_API int sq103_bg_annealer_set_checkpoint(void *handle, const int8_t *q0, const int8_t *q1, int m, int N0,
+                                               int N1, unsigned long long seed, uint32_t step);
 SQ103_API int sq103_bg_annealer_set_trace(void *handle, int enable);
 SQ103_API int sq103_bg_annealer_get_trace(void *handle, uint32_t *bits, int nwords);
 

@@ -55,6 +55,15 @@ __global__ void sym_check_kernel(const float *W, int N, int ld, int *bad) {
     if (__syncthreads_or(mismatch) && tx == 0 && ty == 0) atomicOr(bad, 1);
 }
 
+// host check of int8 bits (0 / 1) or spins (-1 / +1)
+static void check_values(const int8_t *v, size_t n, bool spins, const char *fn) {
+    for (size_t i = 0; i < n; ++i) {
+        const int8_t a = v[i];
+        if (spins ? (a != 1 && a != -1) : (a != 0 && a != 1))
+            sq::throwError("%s, %s must be %s, got %d.", fn, spins ? "q" : "x", spins ? "-1 or +1" : "0 or 1", (int)a);
+    }
+}
+
 class DeviceImpl : public sq::cuda::Device {
 public:
     explicit DeviceImpl(int devNo) { initialize(devNo < 0 ? 0 : devNo); }
@@ -298,6 +307,37 @@ public:
     void rngState(unsigned long long *s, uint32_t *step) const {
         *s = seed_;
         *step = step_;
+    }
+    // Checkpoint (no counterpart in the reference, whose cuRAND generator state
+    // cannot be exported): the spins and resident local fields of every
+    // trotter, the Philox key and step counter, and the steps since the last
+    // field refresh.  Restored into a prepared annealer of the same problem,
+    // algorithm and trotter count, the run continues bit for bit as the
+    // annealer the checkpoint was taken from.
+    void getCheckpoint(int8_t *q, float *F, unsigned long long *s, uint32_t *step, int *since) {
+        throwErrorIfQNotSet();
+        checkStatus();
+        SQ_CHECK(cudaMemcpyAsync(q, d_q_.p, (size_t)m_ * N_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(F, d_F_.p, sizeof(float) * m_ * N_, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        *s = seed_;
+        *step = step_;
+        *since = stepsSinceRefresh_;
+    }
+    void setCheckpoint(const int8_t *q, const float *F, int m, int N, unsigned long long s, uint32_t step, int since) {
+        throwErrorIfNotPrepared();
+        throwErrorIf(m != m_ || N != N_, "%s, Shape does not match: (%d, %d) for an annealer of (%d, %d).", __func__, m,
+                     N, m_, N_);
+        throwErrorIf(since < 0 || since > refreshPeriod_, "%s, steps since the field refresh out of range.", __func__);
+        check_values(q, (size_t)m_ * N_, true, __func__);
+        SQ_CHECK(cudaMemcpyAsync(d_q_.p, q, (size_t)m_ * N_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_F_.p, F, sizeof(float) * m_ * N_, cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();
+        seed_ = s;
+        step_ = step;
+        stepsSinceRefresh_ = since;
+        setState(solRandSeedGiven);
+        setState(solQSet);
     }
     void setTrace(bool on) { trace_ = on; }
     void getTrace(uint32_t *bits, int nwords) {
@@ -682,6 +722,32 @@ public:
     void rngState(unsigned long long *s, uint32_t *step) const {
         *s = seed_;
         *step = step_;
+    }
+    // Checkpoint: the spins of every trotter and the Philox key and step
+    // counter (the fields are recomputed from the spins every half step, so
+    // nothing else carries over).  Restored into a prepared annealer of the same
+    // problem, algorithm and trotter count, the run continues bit for bit.
+    void getCheckpoint(int8_t *q0, int8_t *q1, unsigned long long *s, uint32_t *step) {
+        throwErrorIfQNotSet();
+        SQ_CHECK(cudaMemcpyAsync(q0, d_q0_.p, (size_t)m_ * N0_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(q1, d_q1_.p, (size_t)m_ * N1_, cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        *s = seed_;
+        *step = step_;
+    }
+    void setCheckpoint(const int8_t *q0, const int8_t *q1, int m, int N0, int N1, unsigned long long s,
+                       uint32_t step) {
+        throwErrorIfNotPrepared();
+        throwErrorIf(m != m_ || N0 != N0_ || N1 != N1_, "%s, Shape does not match.", __func__);
+        check_values(q0, (size_t)m_ * N0_, true, __func__);
+        check_values(q1, (size_t)m_ * N1_, true, __func__);
+        SQ_CHECK(cudaMemcpyAsync(d_q0_.p, q0, (size_t)m_ * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_q1_.p, q1, (size_t)m_ * N1_, cudaMemcpyHostToDevice, st_.get()));
+        st_.sync();
+        seed_ = s;
+        step_ = step;
+        setState(solRandSeedGiven);
+        setState(solQSet);
     }
     void setTrace(bool on) { trace_ = on; }
     void getTrace(uint32_t *bits, int nwords) {
@@ -1418,14 +1484,6 @@ private:
 // zero x gives exactly 0.  Bits must be 0 / 1 and spins -1 / +1 (checked).
 // Rows are processed in chunks that keep the FP64 scratch under kFormulaScratch.
 static constexpr size_t kFormulaScratch = (size_t)1 << 25;  // doubles
-
-static void check_values(const int8_t *v, size_t n, bool spins, const char *fn) {
-    for (size_t i = 0; i < n; ++i) {
-        const int8_t a = v[i];
-        if (spins ? (a != 1 && a != -1) : (a != 0 && a != 1))
-            sq::throwError("%s, %s must be %s, got %d.", fn, spins ? "q" : "x", spins ? "-1 or +1" : "0 or 1", (int)a);
-    }
-}
 
 // real-typed rows (the reference's bit / spin vectors) -> int8, checked
 template <class Row>

@@ -207,6 +207,31 @@ class DenseGraphAnnealer(_Handle):
         self._call('get_rng_state', ctypes.byref(s), ctypes.byref(st))
         return s.value, st.value
 
+    def get_checkpoint(self):
+        """The annealing state as a dict of numpy values (numpy.savez stores it):
+        spins q (m x N int8), resident local fields F (m x N float32), the Philox
+        seed and step counter, and the steps since the last field refresh.
+        No counterpart in the reference."""
+        N, m = self.get_problem_size(), self._m()
+        q = np.empty((m, N), np.int8)
+        F = np.empty((m, N), np.float32)
+        s, st, since = ctypes.c_ulonglong(), ctypes.c_uint32(), ctypes.c_int()
+        self._call('get_checkpoint', ptr(q), ptr(F), ctypes.byref(s), ctypes.byref(st), ctypes.byref(since))
+        return {'q': q, 'F': F, 'seed': np.uint64(s.value), 'step': np.uint32(st.value),
+                'since_refresh': np.int32(since.value)}
+
+    def set_checkpoint(self, state):
+        """Restores get_checkpoint()'s state into this prepared annealer (same
+        problem, algorithm and n_trotters): annealing then continues bit for bit
+        as in the annealer the state was taken from."""
+        q = np.ascontiguousarray(state['q'], np.int8)
+        F = np.ascontiguousarray(state['F'], np.float32)
+        if q.ndim != 2 or F.shape != q.shape:
+            raise RuntimeError("checkpoint q and F must be matrices of the same shape.")
+        self._call('set_checkpoint', ptr(q), ptr(F), _c_int(q.shape[0]), _c_int(q.shape[1]),
+                   ctypes.c_ulonglong(int(state['seed'])), ctypes.c_uint32(int(state['step'])),
+                   _c_int(int(state['since_refresh'])))
+
     def set_trace(self, enable):
         self._call('set_trace', _c_int(1 if enable else 0))
 
@@ -342,6 +367,29 @@ class BipartiteGraphAnnealer(_Handle):
         s, st = ctypes.c_ulonglong(), ctypes.c_uint32()
         self._call('get_rng_state', ctypes.byref(s), ctypes.byref(st))
         return s.value, st.value
+
+    def get_checkpoint(self):
+        """The annealing state as a dict of numpy values (numpy.savez stores it):
+        spins q0 (m x N0) and q1 (m x N1), int8, and the Philox seed and step
+        counter.  No counterpart in the reference."""
+        N0, N1 = self.get_problem_size()
+        m = self._m()
+        q0 = np.empty((m, N0), np.int8)
+        q1 = np.empty((m, N1), np.int8)
+        s, st = ctypes.c_ulonglong(), ctypes.c_uint32()
+        self._call('get_checkpoint', ptr(q0), ptr(q1), ctypes.byref(s), ctypes.byref(st))
+        return {'q0': q0, 'q1': q1, 'seed': np.uint64(s.value), 'step': np.uint32(st.value)}
+
+    def set_checkpoint(self, state):
+        """Restores get_checkpoint()'s state into this prepared annealer (same
+        problem, algorithm and n_trotters); annealing continues bit for bit."""
+        q0 = np.ascontiguousarray(state['q0'], np.int8)
+        q1 = np.ascontiguousarray(state['q1'], np.int8)
+        if q0.ndim != 2 or q1.ndim != 2 or q0.shape[0] != q1.shape[0]:
+            raise RuntimeError("checkpoint q0 and q1 must be matrices with the same number of rows.")
+        self._call('set_checkpoint', ptr(q0), ptr(q1), _c_int(q0.shape[0]), _c_int(q0.shape[1]),
+                   _c_int(q1.shape[1]), ctypes.c_ulonglong(int(state['seed'])),
+                   ctypes.c_uint32(int(state['step'])))
 
     def set_trace(self, enable):
         self._call('set_trace', _c_int(1 if enable else 0))
