@@ -7,8 +7,9 @@ problems, with the sqaod solver API.
 The compute path is libsqaod_gb300.so (built in-tree by sqaod_gb300.build);
 there is no CPU fallback.
 """
-from .common import (algorithm, anneal, bit_from_spin, bit_to_spin, create_bitset_sequence,
-                     generate_random_symmetric_W, maximize, minimize, randomize_spin, symmetrize)
+from .common import (Summary, algorithm, anneal, bit_from_spin, bit_to_spin, create_bitset_sequence,
+                     generate_random_symmetric_W, make_summary, maximize, minimize, randomize_spin, symmetrize,
+                     unique_x)
 from ._lib import SqaodError
 
 __version__ = "1.0.3"

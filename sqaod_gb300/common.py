@@ -182,5 +182,41 @@ def anneal(annealer, Ginit=5., Gfin=0.01, beta=1. / 0.02, tau=0.99, n_repeat=10,
     return best_E, best_x
 
 
+def _bits_key(x):
+    """Sort key of a solution: a bit vector, or an (x0, x1) pair ordered by x1 first."""
+    if isinstance(x, (tuple, list)):
+        return tuple(int(v) for part in reversed(x) for v in np.asarray(part).ravel())
+    return tuple(int(v) for v in np.asarray(x).ravel())
+
+
+def unique_x(xlist):
+    """The distinct solutions of xlist in ascending bit order, each once
+    (sqaodpy/sqaod/common/summary.py:39-48)."""
+    out = []
+    for x in sorted(xlist, key=_bits_key):
+        if not out or _bits_key(out[-1]) != _bits_key(x):
+            out.append(x)
+    return out
+
+
+class Summary:
+    """The best energy of a solved problem and its distinct best solutions
+    (sqaodpy/sqaod/common/summary.py:51-69): `E` and `xlist`."""
+
+    def __init__(self, solver=None):
+        if solver is not None:
+            self.summarize(solver)
+
+    def summarize(self, solver):
+        E = np.asarray(solver.get_E())
+        xs = solver.get_x()
+        self.E = solver.get_optimize_dir().best(E)
+        self.xlist = unique_x([xs[i] for i in range(E.shape[0]) if E[i] == self.E])
+
+
+def make_summary(solver=None):
+    return Summary(solver)
+
+
 def is_scalar(v):
     return isinstance(v, numbers.Number)

@@ -90,7 +90,9 @@ void unpackBitSet(BitSet *unpacked, PackedBitSet packed, int N) {
 
 BitSet x_from_q(const BitSet &q) {
     BitSet x(q.size);
-    for (SizeType i = 0; i < q.size; ++i) x(i) = (char)((q(i) + 1) / 2);
+    // spins are read as signed bytes: plain char is unsigned on some targets
+    // (aarch64), where -1 would otherwise read as 255
+    for (SizeType i = 0; i < q.size; ++i) x(i) = (char)(((int)(signed char)q(i) + 1) / 2);
     return x;
 }
 

@@ -141,6 +141,26 @@ def test_known_energies(sq):
     assert b.get_E()[0] == 4 * 4 + 4 + 4
 
 
+def test_get_x_is_the_bits_of_the_spins(sq):
+    """x = (q + 1) / 2 on every target: char is unsigned on aarch64, where a
+    spin read as plain char would turn -1 into 255."""
+    rng = np.random.default_rng(0)
+    a = sq.cuda.dense_graph_annealer(rand_sym(rng, 12), sq.minimize, n_trotters=3)
+    a.seed(1)
+    a.prepare()
+    a.randomize_spin()
+    for q, x in zip(a.get_q(), a.get_x()):
+        assert set(np.unique(q)) <= {-1, 1} and np.array_equal(x, (q + 1) // 2)
+    b = sq.cuda.bipartite_graph_annealer(rng.uniform(-1, 1, 5).astype(np.float32),
+                                         rng.uniform(-1, 1, 7).astype(np.float32),
+                                         rng.uniform(-1, 1, (7, 5)).astype(np.float32), n_trotters=2)
+    b.seed(2)
+    b.prepare()
+    b.randomize_spin()
+    for (q0, q1), (x0, x1) in zip(b.get_q(), b.get_x()):
+        assert np.array_equal(x0, (q0 + 1) // 2) and np.array_equal(x1, (q1 + 1) // 2)
+
+
 def test_bipartite_formulas_golden(sq, golden):
     g = golden
     b = sq.cuda.bipartite_graph_annealer(g["bg_b0"], g["bg_b1"], g["bg_W"])
