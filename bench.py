@@ -408,6 +408,8 @@ def run_batched(args, world):
     for (N, m, seed), W in zip(work, Ws):
         b.add(W, m, sq.minimize, seed)
     b.set_schedule(G, BETA)
+    if args.multicta_min_n is not None:
+        b.set_multicta_min_n(args.multicta_min_n)
     b.prepare()
     torch.cuda.synchronize()
     t_add = time.perf_counter() - t_add
@@ -454,7 +456,9 @@ def run_batched(args, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (W uniform[-1,1] symmetric, seed 1000 + i)",
             "config": {"workload": "1024 dense instances, N log-uniform [64, 2048], m in {8..128}, coloring, "
-                                   "beta=50, %d steps of G=5*0.99^k" % steps, "smem_per_cta": smem},
+                                   "beta=50, %d steps of G=5*0.99^k" % steps, "smem_per_cta": smem,
+                       "multicta_min_n": 1024 if args.multicta_min_n is None else args.multicta_min_n,
+                       "multicta_instances": b.multicta_count()},
             "batched": {"seconds": t_batch, "solves_per_s": len(work) / t_batch, "setup_s": t_add,
                         "results_s": t_out, "seconds_with_setup": t_total,
                         "solves_per_s_with_setup": len(work) / t_total, "autotune_s": t_tune,
@@ -751,6 +755,8 @@ def main():
     ap.add_argument("--check", type=int, default=16, help="served mode: requests compared with the plain path")
     ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")
     ap.add_argument("--plain-sample", type=int, default=16, help="batched mode: instances solved on the plain path")
+    ap.add_argument("--multicta-min-n", type=int, default=None,
+                    help="batched mode: instances of at least this N take the one-CTA-per-trotter sweep (default 1024)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -352,8 +352,9 @@ SQ103_API int sq103_bg_bf_search_range(void *handle, unsigned long long *curX0, 
 SQ103_API int sq103_bg_bf_search(void *handle);
 
 /* ------------------------------------- handle layer: batched annealer */
-/* Many independent dense instances annealed in lock-step, one persistent
- * launch per step (replayed from a CUDA graph when useGraph != 0).  No
+/* Many independent dense instances annealed in lock-step: one persistent
+ * launch per step for the smaller instances (replayed from a CUDA graph when
+ * useGraph != 0), packed one-CTA-per-trotter launches for the larger ones.  No
  * counterpart method table in the reference; each instance follows exactly
  * the rules of sq103_dg_annealer (same seed -> same result).  Coloring
  * algorithm (SA when m == 1). */
@@ -363,6 +364,13 @@ SQ103_API int sq103_dense_batch_add(void *handle, const float *W, int N, int m, 
                                     unsigned long long seed, int *index);
 SQ103_API int sq103_dense_batch_set_schedule(void *handle, const float *G, const float *beta, int nSteps);
 SQ103_API int sq103_dense_batch_prepare(void *handle);
+/* Instances of at least N spins (m >= 2, fitting the device) are stepped by the
+ * one-CTA-per-trotter sweep in packed cooperative launches, the rest by the
+ * persistent batch kernel; both give the same results.  Default 1024; 0 keeps
+ * every instance on the persistent kernel.  Takes effect at the next prepare. */
+SQ103_API int sq103_dense_batch_set_multicta_min_n(void *handle, int N);
+/* instances on the one-CTA-per-trotter sweep since the last prepare */
+SQ103_API int sq103_dense_batch_multicta_count(void *handle, int *n);
 SQ103_API int sq103_dense_batch_autotune(void *handle, int trialSteps, int *smemBytes);
 SQ103_API int sq103_dense_batch_anneal(void *handle, int nSteps, int useGraph);
 SQ103_API int sq103_dense_batch_sync(void *handle);

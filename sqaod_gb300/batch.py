@@ -56,6 +56,17 @@ class DenseBatchAnnealer:
     def prepare(self):
         self._call("prepare")
 
+    def set_multicta_min_n(self, N):
+        """Instances of at least N spins run on the one-CTA-per-trotter sweep
+        (packed launches); 0 keeps all on the persistent kernel.  Default 1024;
+        results do not depend on it.  Takes effect at the next prepare()."""
+        self._call("set_multicta_min_n", ctypes.c_int(N))
+
+    def multicta_count(self):
+        n = ctypes.c_int()
+        self._call("multicta_count", ctypes.byref(n))
+        return n.value
+
     def autotune(self, trial_steps=2):
         s = ctypes.c_int()
         self._call("autotune", ctypes.c_int(trial_steps), ctypes.byref(s))

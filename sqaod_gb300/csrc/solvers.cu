@@ -1227,11 +1227,20 @@ private:
 class DenseBatch : public sq::NullBase {
 public:
     static constexpr int kRefreshPeriod = 8;
+    static constexpr int kPackMax = 8;           // instances per packed launch
+    static constexpr int kDefaultMultiMinN = 1024;
 
+    // Instances of at least multiMinN_ spins (with m >= 2 that fit the device) run
+    // on the one-CTA-per-trotter sweep in packed cooperative launches: its decider
+    // takes 32 iterations per round trip, where the persistent one-CTA kernel
+    // takes one per colour phase, and the serial chain of the largest instances
+    // sets the batch's step time.  Both kernels give bit-identical results.
     struct Inst {
-        int N, m;
+        int N, m, ldJ;  // J rows on a 16-byte stride (the one-CTA-per-trotter sweep reads them as float4)
+        bool multi = false;
         unsigned long long seed;
-        DevBuf<unsigned char> mem;
+        DevBuf<unsigned char> mem, ws;
+        unsigned long long wsBytes = 0;
         float *J, *h, *c32, *F;
         double *c64;
         int8_t *q;
@@ -1249,9 +1258,10 @@ public:
         Inst &in = *insts_.back();
         in.N = N;
         in.m = m;
+        in.ldJ = (N + 3) & ~3;
         in.seed = seed;
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-        size_t oJ = 0, oh = oJ + al((size_t)N * N * 4), oc = oh + al((size_t)N * 4), oc64 = oc + 256,
+        size_t oJ = 0, oh = oJ + al((size_t)N * in.ldJ * 4), oc = oh + al((size_t)N * 4), oc64 = oc + 256,
                oF = oc64 + 256, oq = oF + al((size_t)m * N * 4), total = oq + al((size_t)m * N);
         in.mem.ensure(total);
         unsigned char *b = in.mem.p;
@@ -1264,7 +1274,9 @@ public:
         dW_.ensure((size_t)N * N);
         scratch_.ensure(N);
         SQ_CHECK(cudaMemcpyAsync(dW_.p, W, sizeof(float) * N * N, cudaMemcpyHostToDevice, st_.get()));
-        SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, optimize, in.h, in.J, N, in.c32, in.c64, scratch_.p, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(in.J, 0, sizeof(float) * N * in.ldJ, st_.get()));  // zero row padding
+        SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, optimize, in.h, in.J, in.ldJ, in.c32, in.c64, scratch_.p,
+                                         st_.get()));
         st_.sync();
         optimize_.push_back(optimize);
         return (int)insts_.size() - 1;
@@ -1284,13 +1296,22 @@ public:
     void prepare() {
         throwErrorIf(insts_.empty(), "no instance added.");
         throwErrorIf(nSched_ <= 0, "set a schedule before prepare().");
-        const int n = (int)insts_.size();
-        std::vector<sq103_dense_task> tasks(n);
+        const int nAll = (int)insts_.size();
+        std::vector<sq103_dense_task> tasks;
+        std::vector<Inst *> smallInsts;
+        multi_.clear();
         int maxN = 0, maxM = 0;
-        for (int i = 0; i < n; ++i) {
+        for (int i = 0; i < nAll; ++i) {
             Inst &in = *insts_[i];
             SQ_CHECK(sq103_randomize_spins(in.q, in.N, in.m, in.seed, 0, 0, st_.get()));
-            SQ_CHECK(sq103_dense_field_refresh(in.J, in.N, in.q, in.F, in.N, in.m, st_.get()));
+            SQ_CHECK(sq103_dense_field_refresh(in.J, in.ldJ, in.q, in.F, in.N, in.m, st_.get()));
+            in.multi = multiMinN_ > 0 && in.N >= multiMinN_ && in.m >= 2 && sq103_dense_multicta_ok(in.N, in.m, kColoring);
+            if (in.multi) {
+                in.wsBytes = sq103_dense_ws_bytes(in.N, in.m, kRefreshPeriod);
+                in.ws.ensure(in.wsBytes);
+                multi_.push_back(&in);
+                continue;
+            }
             sq103_dense_task t = {};
             t.J = in.J;
             t.h = in.h;
@@ -1303,27 +1324,38 @@ public:
             t.step0 = 1;  // step 0 of the Philox counter is the randomisation
             t.N = in.N;
             t.m = in.m;
-            t.ldJ = in.N;
+            t.ldJ = in.ldJ;
             t.algo = in.m == 1 ? kSANaive : kColoring;
             t.nSteps = nSched_;
-            tasks[i] = t;
+            tasks.push_back(t);
+            smallInsts.push_back(&in);
             maxN = std::max(maxN, in.N);
             maxM = std::max(maxM, in.m);
         }
+        // packed launches take instances of similar size together
+        std::stable_sort(multi_.begin(), multi_.end(), [](const Inst *a, const Inst *b) { return a->N < b->N; });
         // largest instances first: the queue then balances the tail
+        const int n = (int)tasks.size();
+        nSmall_ = n;
         std::vector<int> order(n);
         for (int i = 0; i < n; ++i) order[i] = i;
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            return (long long)insts_[a]->N * insts_[a]->m > (long long)insts_[b]->N * insts_[b]->m;
+            return (long long)smallInsts[a]->N * smallInsts[a]->m > (long long)smallInsts[b]->N * smallInsts[b]->m;
         });
-        dTasks_.ensure(n);
-        dOrder_.ensure(n);
-        dPos_.ensure(n);
+        const int nAlloc = std::max(n, 1);
+        dTasks_.ensure(nAlloc);
+        dOrder_.ensure(nAlloc);
+        dPos_.ensure(nAlloc);
         dQueue_.ensure(2);
-        SQ_CHECK(cudaMemcpyAsync(dTasks_.p, tasks.data(), sizeof(sq103_dense_task) * n, cudaMemcpyHostToDevice, st_.get()));
-        SQ_CHECK(cudaMemcpyAsync(dOrder_.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st_.get()));
-        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+        dStatus_.ensure(1);
+        if (n > 0) {
+            SQ_CHECK(cudaMemcpyAsync(dTasks_.p, tasks.data(), sizeof(sq103_dense_task) * n, cudaMemcpyHostToDevice,
+                                     st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(dOrder_.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st_.get()));
+        }
+        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * nAlloc, st_.get()));
         SQ_CHECK(cudaMemsetAsync(dQueue_.p, 0, sizeof(int) * 2, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(dStatus_.p, 0, sizeof(int), st_.get()));
         st_.sync();
         pos_ = 0;
         if (smem_ < 0) chooseConfig(-1);
@@ -1347,7 +1379,7 @@ public:
         smem_ = smemBytes < 0 ? std::min(maxS, 96 * 1024) : std::min(smemBytes, maxS);
         smem_ = std::max(smem_, minS);
         int per = std::max(1, sq103_dense_batch_ctas_per_sm(smem_));
-        grid_ = std::max(1, std::min((int)insts_.size(), per * sms));
+        grid_ = std::max(1, std::min(std::max(nSmall_, 1), per * sms));
         if (graph_) {
             cudaGraphExecDestroy(graph_);
             graph_ = nullptr;
@@ -1376,7 +1408,7 @@ public:
         for (int c : cands) {
             if (c > maxS) continue;
             chooseConfig(c);
-            SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+            SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * std::max(nSmall_, 1), st_.get()));
             SQ_CHECK(cudaEventRecord(e0, st_.get()));
             for (int s = 0; s < trialSteps; ++s) launchOne();
             SQ_CHECK(cudaEventRecord(e1, st_.get()));
@@ -1395,28 +1427,50 @@ public:
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * n, st_.get()));
+        SQ_CHECK(cudaMemsetAsync(dPos_.p, 0, sizeof(int) * std::max(nSmall_, 1), st_.get()));
         st_.sync();
         chooseConfig(bestS);
         return bestS;
     }
 
-    // nSteps further steps of every instance (bounded by the schedule length)
+    // nSteps further steps of every instance (bounded by the schedule length), in
+    // chunks that end at the field refreshes (every kRefreshPeriod steps, as the
+    // single-instance solver refreshes)
     void anneal(int nSteps, bool useGraph) {
         throwErrorIf(!prepared_, "prepare() first.");
-        for (int s = 0; s < nSteps && pos_ < nSched_; ++s) {
+        int left = std::min(nSteps, nSched_ - pos_);
+        while (left > 0) {
             if (pos_ > 0 && pos_ % kRefreshPeriod == 0) refreshAll();
-            if (useGraph) {
-                if (!graph_) captureStep();
-                SQ_CHECK(cudaGraphLaunch(graph_, st_.get()));
-            } else {
-                launchOne();
+            const int chunk = std::min(left, kRefreshPeriod - pos_ % kRefreshPeriod);
+            for (int s = 0; s < chunk && nSmall_ > 0; ++s) {
+                if (useGraph) {
+                    if (!graph_) captureStep();
+                    SQ_CHECK(cudaGraphLaunch(graph_, st_.get()));
+                } else {
+                    launchOne();
+                }
             }
-            ++pos_;
+            launchMulti(chunk);
+            pos_ += chunk;
+            left -= chunk;
         }
     }
 
-    void sync() { st_.sync(); }
+    void sync() {
+        st_.sync();
+        if (multi_.empty()) return;
+        int status = 0;
+        SQ_CHECK(cudaMemcpy(&status, dStatus_.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status != 0) throw_cuda(status, "one-CTA-per-trotter batch sweep");
+    }
+
+    // instances of at least N spins take the one-CTA-per-trotter sweep (0: none); before prepare()
+    void setMultiMinN(int N) {
+        throwErrorIf(N < 0, "the size limit must not be negative.");
+        multiMinN_ = N;
+        prepared_ = false;
+    }
+    int multiCount() const { return (int)multi_.size(); }
     int size() const { return (int)insts_.size(); }
     int position() const { return pos_; }
     int grid() const { return grid_; }
@@ -1430,8 +1484,8 @@ public:
         const Inst &in = inst(i);
         r_.ensure((size_t)in.m * in.N);
         E64_.ensure(in.m);
-        SQ_CHECK(sq103_dense_energy(in.J, in.N, in.h, in.c64, in.q, in.N, in.m, optimize_[i], r_.p, E64_.p, nullptr,
-                                    st_.get()));
+        SQ_CHECK(sq103_dense_energy(in.J, in.ldJ, in.h, in.c64, in.q, in.N, in.m, optimize_[i], r_.p, E64_.p,
+                                    nullptr, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(E, E64_.p, sizeof(double) * in.m, cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
     }
@@ -1444,12 +1498,49 @@ public:
 
 private:
     void launchOne() {
-        SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, (int)insts_.size(), nullptr, dOrder_.p, dPos_.p, dQueue_.p, 1, grid_, smem_,
+        SQ_CHECK(sq103_dense_batch_launch(dTasks_.p, nSmall_, nullptr, dOrder_.p, dPos_.p, dQueue_.p, 1, grid_, smem_,
                                           st_.get()));
     }
 
+    // `chunk` steps of the large instances from pos_: packed cooperative launches of
+    // instances of similar size, as many trotters as can be resident at once
+    void launchMulti(int chunk) {
+        std::vector<sq103_dense_task> pack;
+        int packM = 0, packN = 0;
+        auto flush = [&]() {
+            if (!pack.empty()) SQ_CHECK(sq103_dense_anneal_pack(pack.data(), (int)pack.size(), st_.get()));
+            pack.clear();
+            packM = packN = 0;
+        };
+        for (Inst *in : multi_) {
+            sq103_dense_task t = {};
+            t.J = in->J;
+            t.h = in->h;
+            t.q = in->q;
+            t.F = in->F;
+            t.G = sched_.p + pos_;
+            t.beta = sched_.p + nSched_ + pos_;
+            t.status = dStatus_.p;
+            t.seed = in->seed;
+            t.step0 = 1 + (uint32_t)pos_;  // step 0 of the Philox counter is the randomisation
+            t.N = in->N;
+            t.m = in->m;
+            t.ldJ = in->ldJ;
+            t.algo = kColoring;
+            t.nSteps = chunk;
+            t.ws = in->ws.p;
+            t.wsBytes = in->wsBytes;
+            const int N2 = std::max(packN, in->N);
+            if ((int)pack.size() == kPackMax || packM + in->m > sq103_dense_multicta_capacity(N2)) flush();
+            pack.push_back(t);
+            packM += in->m;
+            packN = std::max(packN, in->N);
+        }
+        flush();
+    }
+
     void refreshAll() {
-        for (auto &p : insts_) SQ_CHECK(sq103_dense_field_refresh(p->J, p->N, p->q, p->F, p->N, p->m, st_.get()));
+        for (auto &p : insts_) SQ_CHECK(sq103_dense_field_refresh(p->J, p->ldJ, p->q, p->F, p->N, p->m, st_.get()));
     }
 
     void captureStep() {
@@ -1467,9 +1558,10 @@ private:
     DevBuf<float> dW_, sched_;
     DevBuf<double> scratch_, r_, E64_;
     DevBuf<sq103_dense_task> dTasks_;
-    DevBuf<int> dOrder_, dPos_, dQueue_;
+    DevBuf<int> dOrder_, dPos_, dQueue_, dStatus_;
+    std::vector<Inst *> multi_;  // the instances on the one-CTA-per-trotter sweep, by N
     cudaGraphExec_t graph_ = nullptr;
-    int nSched_ = 0, pos_ = 0, grid_ = 1, smem_ = -1;
+    int nSched_ = 0, pos_ = 0, grid_ = 1, smem_ = -1, nSmall_ = 0, multiMinN_ = kDefaultMultiMinN;
     bool prepared_ = false;
 };
 

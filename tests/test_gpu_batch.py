@@ -29,8 +29,8 @@ def _problems(k, seed=0):
     return out
 
 
-@pytest.mark.parametrize("use_graph", [True, False])
-def test_batch_equals_single(use_graph):
+@pytest.mark.parametrize("use_graph,min_n", [(True, None), (False, None), (True, 0), (False, 64), (True, 512)])
+def test_batch_equals_single(use_graph, min_n):
     import sqaod_gb300 as sq
     from sqaod_gb300.batch import DenseBatchAnnealer
     probs = _problems(12)
@@ -39,9 +39,17 @@ def test_batch_equals_single(use_graph):
     for W, m, seed in probs:
         b.add(W, m, sq.minimize, seed)
     b.set_schedule(G, 30.0)
+    if min_n is not None:
+        b.set_multicta_min_n(min_n)
     b.prepare()
+    # instances of at least min_n spins (default 1024) and m >= 2 take the packed launches
+    limit = 1024 if min_n is None else min_n
+    expect = sum(1 for W, m, _ in probs if limit > 0 and W.shape[0] >= limit and m >= 2)
+    assert b.multicta_count() == expect
     b.autotune(2)
-    b.anneal(len(G), use_graph=use_graph)
+    # uneven calls: chunks must still end at the field refreshes
+    b.anneal(5, use_graph=use_graph)
+    b.anneal(len(G) - 5, use_graph=use_graph)
     assert b.info()["position"] == len(G)
     for i, (W, m, seed) in enumerate(probs):
         # one trotter runs simulated annealing in the batch
