@@ -189,6 +189,24 @@ SQ103_API int sq103_bipartite_energy(const float *J, const float *h0, const floa
                                      const int8_t *q0, const int8_t *q1, int N0, int N1, int m,
                                      int maximize, double *r_scratch, double *E64, float *E32,
                                      void *stream);
+
+/* ------------------------------------- kernel layer: FP64 formula kernels */
+/* The formulas with real = double (sqaodc/cuda/DeviceFormulas.cpp:24-140 of
+ * the <double> instantiation): FP64 inputs, FP64 sums in a fixed order.
+ * Dense: W, J N x N row-major; scratch N doubles.  Energies: E[y] =
+ * sign (-c - h q_y^T - q_y J q_y^T), sign -1 when maximize; h may be NULL
+ * (zero); a QUBO energy x W x^T is the call with J = W, h = NULL, c = 0,
+ * maximize = 1.  Bipartite: W, J N1 x N0; scratch N0 + 2 N1 doubles. */
+SQ103_API int sq103_dense_hamiltonian64(const double *W, int N, double *h, double *J, double *c, double *scratch,
+                                        void *stream);
+SQ103_API int sq103_dense_energy64(const double *J, const double *h, double c, const int8_t *q, int N, int m,
+                                   int maximize, double *E, void *stream);
+SQ103_API int sq103_bipartite_hamiltonian64(const double *b0, const double *b1, const double *W, int N0, int N1,
+                                            double *h0, double *h1, double *J, double *c, double *scratch,
+                                            void *stream);
+SQ103_API int sq103_bipartite_energy64(const double *J, const double *h0, const double *h1, double c,
+                                       const int8_t *q0, const int8_t *q1, int N0, int N1, int m, int maximize,
+                                       double *E, void *stream);
 /* nSteps annealOneStep of one bipartite instance
  * (CUDABipartiteGraphAnnealer::annealOneStepSQA/SA, :539-625) */
 SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task, void *stream);
@@ -416,6 +434,30 @@ SQ103_API int sq103_bg_formulas_calculate_hamiltonian(void *handle, const float 
 SQ103_API int sq103_bg_formulas_calculate_E_from_spin(void *handle, const float *h0, const float *h1,
                                                       const float *J, float c, int N0, int N1, const int8_t *q0,
                                                       const int8_t *q1, int m, double *E);
+/* The same formula sets with real = double (the reference's <double>
+ * instantiation of CUDADenseGraphFormulas / CUDABipartiteGraphFormulas):
+ * arguments as above with double matrices, vectors and c; FP64 kernels. */
+SQ103_API int sq103_dg_formulas64_new(void **handle);
+SQ103_API int sq103_dg_formulas64_delete(void *handle);
+SQ103_API int sq103_dg_formulas64_calculate_E(void *handle, const double *W, int N, const int8_t *x, int m,
+                                              double *E);
+SQ103_API int sq103_dg_formulas64_calculate_hamiltonian(void *handle, const double *W, int N, double *h,
+                                                        double *J, double *c);
+SQ103_API int sq103_dg_formulas64_calculate_E_from_spin(void *handle, const double *h, const double *J, double c,
+                                                        int N, const int8_t *q, int m, double *E);
+SQ103_API int sq103_bg_formulas64_new(void **handle);
+SQ103_API int sq103_bg_formulas64_delete(void *handle);
+SQ103_API int sq103_bg_formulas64_calculate_E(void *handle, const double *b0, const double *b1, const double *W,
+                                              int N0, int N1, const int8_t *x0, const int8_t *x1, int m, double *E);
+SQ103_API int sq103_bg_formulas64_calculate_E_2d(void *handle, const double *b0, const double *b1,
+                                                 const double *W, int N0, int N1, const int8_t *x0, int m0,
+                                                 const int8_t *x1, int m1, double *E);
+SQ103_API int sq103_bg_formulas64_calculate_hamiltonian(void *handle, const double *b0, const double *b1,
+                                                        const double *W, int N0, int N1, double *h0, double *h1,
+                                                        double *J, double *c);
+SQ103_API int sq103_bg_formulas64_calculate_E_from_spin(void *handle, const double *h0, const double *h1,
+                                                        const double *J, double c, int N0, int N1,
+                                                        const int8_t *q0, const int8_t *q1, int m, double *E);
 
 /* ------------------------------------------- handle layer: request server */
 /* Continuous batching of anneal requests of mixed size and type (no

@@ -322,3 +322,151 @@ SQ103_API int sq103_ring_dot(const int8_t *q, int N, int m, long long *out, void
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ FP64 formula sets
+// The double-precision formula kernels (sqaodc/cuda/DeviceFormulas.cpp:24-140
+// instantiated with real = double): plain FP64 sums over a fixed thread
+// assignment and reduction tree, so a result does not depend on the launch.
+// Bits (0 / 1) and spins (+-1) times FP64 couplings are exact products.
+namespace sq103 {
+
+// h_i = -1/2 sum_j W_ij, J = -W / 4 with a zero diagonal; rs_i = sum_j W_ij + W_ii
+__global__ void __launch_bounds__(256) dg_hamiltonian64_rows(const double *W, int N, double *h, double *J,
+                                                             double *rs) {
+    __shared__ double red[8];
+    const int i = blockIdx.x;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N; j += 256) {
+        const double w = W[(size_t)i * N + j];
+        s += w;
+        J[(size_t)i * N + j] = i == j ? 0. : -0.25 * w;
+    }
+    const double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        h[i] = -0.5 * t;
+        rs[i] = t + W[(size_t)i * N + i];
+    }
+}
+
+// out = scale * sum v + add (one CTA)
+__global__ void __launch_bounds__(256) sum_scaled64(const double *v, int n, double scale, const double *v2, int n2,
+                                                    double scale2, double *out) {
+    __shared__ double red[8];
+    double s = 0., s2 = 0.;
+    for (int i = threadIdx.x; i < n; i += 256) s += v[i];
+    for (int i = threadIdx.x; i < n2; i += 256) s2 += v2[i];
+    const double t = block_sum_f64<256>(s, red);
+    const double t2 = block_sum_f64<256>(s2, red);
+    if (threadIdx.x == 0) *out = scale * t + scale2 * t2;
+}
+
+// bipartite, W N1 x N0: h1_i = -1/4 sum_j W_ij - b1_i / 2, J = -W / 4, rs_i = sum_j W_ij
+__global__ void __launch_bounds__(256) bg_hamiltonian64_rows(const double *W, const double *b1, int N0, double *h1,
+                                                             double *J, double *rs) {
+    __shared__ double red[8];
+    const int i = blockIdx.x;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N0; j += 256) {
+        const double w = W[(size_t)i * N0 + j];
+        s += w;
+        J[(size_t)i * N0 + j] = -0.25 * w;
+    }
+    const double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) {
+        h1[i] = -0.25 * t - 0.5 * b1[i];
+        rs[i] = t;
+    }
+}
+
+// h0_j = -1/4 sum_i W_ij - b0_j / 2 (a thread per column, rows ascending)
+__global__ void bg_hamiltonian64_cols(const double *W, const double *b0, int N0, int N1, double *h0) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N0) return;
+    double s = 0.;
+    for (int i = 0; i < N1; ++i) s += W[(size_t)i * N0 + j];
+    h0[j] = -0.25 * s - 0.5 * b0[j];
+}
+
+// E[y] = sign (-c - sum_i q_i (h_i + sum_j J_ij q_j)); h may be null (zero)
+__global__ void __launch_bounds__(256) dense_energy64(const double *J, const double *h, double c, const int8_t *q,
+                                                      int N, double sign, double *E) {
+    __shared__ double red[8];
+    const int y = blockIdx.x;
+    const int8_t *qy = q + (size_t)y * N;
+    double s = 0.;
+    for (int i = threadIdx.x; i < N; i += 256) {
+        const int qi = qy[i];
+        if (qi == 0) continue;
+        const double *Ji = J + (size_t)i * N;
+        double d = 0.;
+        for (int j = 0; j < N; ++j) d += Ji[j] * (double)qy[j];
+        s += (double)qi * ((h ? h[i] : 0.) + d);
+    }
+    const double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) E[y] = sign * (-c - t);
+}
+
+// E[y] = sign (-c - h0.q0 - sum_i q1_i (h1_i + sum_j J_ij q0_j)), J N1 x N0
+__global__ void __launch_bounds__(256) bipartite_energy64(const double *J, const double *h0, const double *h1,
+                                                          double c, const int8_t *q0, const int8_t *q1, int N0,
+                                                          int N1, double sign, double *E) {
+    __shared__ double red[8];
+    const int y = blockIdx.x;
+    const int8_t *a = q0 + (size_t)y * N0, *b = q1 + (size_t)y * N1;
+    double s = 0.;
+    for (int j = threadIdx.x; j < N0; j += 256) s += (double)a[j] * h0[j];
+    for (int i = threadIdx.x; i < N1; i += 256) {
+        const int bi = b[i];
+        if (bi == 0) continue;
+        const double *Ji = J + (size_t)i * N0;
+        double d = 0.;
+        for (int j = 0; j < N0; ++j) d += Ji[j] * (double)a[j];
+        s += (double)bi * (h1[i] + d);
+    }
+    const double t = block_sum_f64<256>(s, red);
+    if (threadIdx.x == 0) E[y] = sign * (-c - t);
+}
+
+}  // namespace sq103
+
+extern "C" {
+
+SQ103_API int sq103_dense_hamiltonian64(const double *W, int N, double *h, double *J, double *c, double *scratch,
+                                        void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (N <= 0) return kErrBadShape;
+    dg_hamiltonian64_rows<<<N, 256, 0, s>>>(W, N, h, J, scratch);
+    sum_scaled64<<<1, 256, 0, s>>>(scratch, N, -0.25, nullptr, 0, 0., c);  // c = -(sum W + tr W) / 4
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_energy64(const double *J, const double *h, double c, const int8_t *q, int N, int m,
+                                   int maximize, double *E, void *stream) {
+    if (N <= 0 || m <= 0) return kErrBadShape;
+    dense_energy64<<<m, 256, 0, (cudaStream_t)stream>>>(J, h, c, q, N, maximize ? -1. : 1., E);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_hamiltonian64(const double *b0, const double *b1, const double *W, int N0, int N1,
+                                            double *h0, double *h1, double *J, double *c, double *scratch,
+                                            void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (N0 <= 0 || N1 <= 0) return kErrBadShape;
+    bg_hamiltonian64_rows<<<N1, 256, 0, s>>>(W, b1, N0, h1, J, scratch);
+    bg_hamiltonian64_cols<<<(N0 + 127) / 128, 128, 0, s>>>(W, b0, N0, N1, h0);
+    // c = -(sum W) / 4 - (sum b0 + sum b1) / 2: the row sums, then b0 and b1 (copied after them)
+    cudaMemcpyAsync(scratch + N1, b0, sizeof(double) * N0, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(scratch + N1 + N0, b1, sizeof(double) * N1, cudaMemcpyDeviceToDevice, s);
+    sum_scaled64<<<1, 256, 0, s>>>(scratch, N1, -0.25, scratch + N1, N0 + N1, -0.5, c);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_energy64(const double *J, const double *h0, const double *h1, double c,
+                                       const int8_t *q0, const int8_t *q1, int N0, int N1, int m, int maximize,
+                                       double *E, void *stream) {
+    if (N0 <= 0 || N1 <= 0 || m <= 0) return kErrBadShape;
+    bipartite_energy64<<<m, 256, 0, (cudaStream_t)stream>>>(J, h0, h1, c, q0, q1, N0, N1, maximize ? -1. : 1., E);
+    return (int)cudaGetLastError();
+}
+
+}  // extern "C"

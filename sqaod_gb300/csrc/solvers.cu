@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <sqaodc/sqaodc.h>
@@ -1566,16 +1567,18 @@ private:
 };
 
 // ============================================================= formulas
-// The CUDA formula sets (sqaodc/cuda/CUDAFormulas.cpp:8-294): each call
-// uploads its host arguments, runs the Hamiltonian or energy kernels of
-// formulas.cu on the object's stream and copies the result back.  Energies
-// are summed in FP64 (the row sums in double-float) and rounded to float only
-// where the interface returns float.  A QUBO energy is the Ising energy kernel
-// run with J = W, h = b, c = 0 and the sign of a maximisation: bits times fp32
-// couplings are exact products, so the result is x W x^T summed in FP64 and a
-// zero x gives exactly 0.  Bits must be 0 / 1 and spins -1 / +1 (checked).
-// Rows are processed in chunks that keep the FP64 scratch under kFormulaScratch.
-static constexpr size_t kFormulaScratch = (size_t)1 << 25;  // doubles
+// The CUDA formula sets (sqaodc/cuda/CUDAFormulas.cpp:8-294), for real = float
+// and real = double: each call uploads its host arguments, runs the
+// Hamiltonian or energy kernels of formulas.cu on the object's stream and
+// copies the result back.  Energies are FP64 (float: fp32 inputs with
+// double-float row sums; double: FP64 throughout) and rounded to real only
+// where the interface returns real.  A QUBO energy is the Ising energy kernel
+// run with J = W, h = b, c = 0 and the sign of a maximisation: bits times the
+// couplings are exact products, so the result is x W x^T to FP64 accuracy and
+// a zero x gives exactly 0.  Bits must be 0 / 1 and spins -1 / +1 (checked).
+// Rows are processed in chunks that keep the device scratch under
+// kFormulaScratch doubles.
+static constexpr size_t kFormulaScratch = (size_t)1 << 25;
 
 // real-typed rows (the reference's bit / spin vectors) -> int8, checked
 template <class Row>
@@ -1583,8 +1586,8 @@ static std::vector<int8_t> rows_to_int8(const Row *rows, int nRows, int len, boo
     std::vector<int8_t> out((size_t)nRows * len);
     for (int r = 0; r < nRows; ++r)
         for (int i = 0; i < len; ++i) {
-            const float v = rows[r](i);
-            throwErrorIf(spins ? (v != 1.f && v != -1.f) : (v != 0.f && v != 1.f), "%s, %s must be %s.", fn,
+            const double v = (double)rows[r](i);
+            throwErrorIf(spins ? (v != 1. && v != -1.) : (v != 0. && v != 1.), "%s, %s must be %s.", fn,
                          spins ? "q" : "x", spins ? "-1 or +1" : "0 or 1");
             out[(size_t)r * len + i] = (int8_t)v;
         }
@@ -1592,32 +1595,50 @@ static std::vector<int8_t> rows_to_int8(const Row *rows, int nRows, int len, boo
 }
 
 // row accessors over the reference's Vector / Matrix types
+template <class real>
 struct VecRow {
-    const sq::VectorType<float> *v;
-    float operator()(int i) const { return v->data[i]; }
+    const sq::VectorType<real> *v;
+    real operator()(int i) const { return v->data[i]; }
 };
+template <class real>
 struct MatRow {
-    const sq::MatrixType<float> *m;
+    const sq::MatrixType<real> *m;
     int r;
-    float operator()(int i) const { return m->data[(size_t)r * m->stride + i]; }
+    real operator()(int i) const { return m->data[(size_t)r * m->stride + i]; }
 };
-static std::vector<MatRow> mat_rows(const sq::MatrixType<float> &m) {
-    std::vector<MatRow> rows;
-    for (int r = 0; r < m.rows; ++r) rows.push_back(MatRow{&m, r});
+template <class real>
+static std::vector<MatRow<real>> mat_rows(const sq::MatrixType<real> &m) {
+    std::vector<MatRow<real>> rows;
+    for (int r = 0; r < m.rows; ++r) rows.push_back(MatRow<real>{&m, r});
     return rows;
 }
+// a matrix with row stride = columns
+template <class real>
+static std::vector<real> dense_copy(const sq::MatrixType<real> &M) {
+    std::vector<real> d((size_t)M.rows * M.cols);
+    for (int i = 0; i < M.rows; ++i)
+        memcpy(d.data() + (size_t)i * M.cols, M.data + (size_t)i * M.stride, sizeof(real) * M.cols);
+    return d;
+}
+template <class real>
+static void to_vector(sq::VectorType<real> *E, const std::vector<double> &e) {
+    E->resize((int)e.size());
+    for (size_t i = 0; i < e.size(); ++i) E->data[i] = (real)e[i];
+}
 
-class DenseFormulas : public sq::cuda::DenseGraphFormulas<float> {
+template <class real>
+class DenseFormulasT : public sq::cuda::DenseGraphFormulas<real> {
 public:
-    typedef sq::MatrixType<float> Matrix;
-    typedef sq::VectorType<float> Vector;
+    typedef sq::MatrixType<real> Matrix;
+    typedef sq::VectorType<real> Vector;
+    static constexpr bool kF64 = std::is_same<real, double>::value;
 
     void assignDevice(sq::cuda::Device &device) override {
         SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
     }
 
     // E[i] = x_i W x_i^T for the m rows of x (int8 bits, row stride N)
-    void quboEnergies(const float *W, int ldW, int N, const int8_t *x, int m, double *E) {
+    void quboEnergies(const real *W, int ldW, int N, const int8_t *x, int m, double *E) {
         check_shape(N, m, __func__);
         throwErrorIf(!sq::isSymmetric(W, (size_t)N, (size_t)ldW), "%s, Matrix is not symmetric.", __func__);
         check_values(x, (size_t)m * N, false, __func__);
@@ -1625,14 +1646,14 @@ public:
     }
 
     // E[i] = -c - h q_i^T - q_i J q_i^T (int8 spins)
-    void isingEnergies(const float *h, const float *J, int ldJ, float c, int N, const int8_t *q, int m, double *E) {
+    void isingEnergies(const real *h, const real *J, int ldJ, real c, int N, const int8_t *q, int m, double *E) {
         check_shape(N, m, __func__);
         throwErrorIf(!sq::isSymmetric(J, (size_t)N, (size_t)ldJ), "%s, Matrix is not symmetric.", __func__);
         check_values(q, (size_t)m * N, true, __func__);
         energies(J, ldJ, h, (double)c, N, q, m, false, E);
     }
 
-    void hamiltonian(const float *W, int ldW, int N, float *h, float *J, float *c) {
+    void hamiltonian(const real *W, int ldW, int N, real *h, real *J, real *c) {
         check_shape(N, 1, __func__);
         throwErrorIf(!sq::isSymmetric(W, (size_t)N, (size_t)ldW), "%s, Matrix is not symmetric.", __func__);
         cudaStream_t s = st_.get();
@@ -1642,63 +1663,64 @@ public:
         dc_.ensure(1);
         dc64_.ensure(1);
         dscr_.ensure(N);
-        SQ_CHECK(cudaMemcpy2DAsync(dW_.p, sizeof(float) * N, W, sizeof(float) * ldW, sizeof(float) * N, N,
+        SQ_CHECK(cudaMemcpy2DAsync(dW_.p, sizeof(real) * N, W, sizeof(real) * ldW, sizeof(real) * N, N,
                                    cudaMemcpyHostToDevice, s));
-        SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, 0, dh_.p, dJ_.p, N, dc_.p, dc64_.p, dscr_.p, s));
-        SQ_CHECK(cudaMemcpyAsync(h, dh_.p, sizeof(float) * N, cudaMemcpyDeviceToHost, s));
-        SQ_CHECK(cudaMemcpyAsync(J, dJ_.p, sizeof(float) * N * N, cudaMemcpyDeviceToHost, s));
-        SQ_CHECK(cudaMemcpyAsync(c, dc_.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+        if constexpr (kF64)
+            SQ_CHECK(sq103_dense_hamiltonian64(dW_.p, N, dh_.p, dJ_.p, dc_.p, dscr_.p, s));
+        else
+            SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, 0, dh_.p, dJ_.p, N, dc_.p, dc64_.p, dscr_.p, s));
+        SQ_CHECK(cudaMemcpyAsync(h, dh_.p, sizeof(real) * N, cudaMemcpyDeviceToHost, s));
+        SQ_CHECK(cudaMemcpyAsync(J, dJ_.p, sizeof(real) * N * N, cudaMemcpyDeviceToHost, s));
+        SQ_CHECK(cudaMemcpyAsync(c, dc_.p, sizeof(real), cudaMemcpyDeviceToHost, s));
         st_.sync();
     }
 
     // ---- the reference's interface
-    void calculate_E(float *E, const Matrix &W, const Vector &x) override {
+    void calculate_E(real *E, const Matrix &W, const Vector &x) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         throwErrorIf(W.rows != W.cols || x.size != W.cols, "%s, Shape does not match.", __func__);
-        VecRow r{&x};
+        VecRow<real> r{&x};
         std::vector<int8_t> xi = rows_to_int8(&r, 1, x.size, false, __func__);
         double e;
         quboEnergies(W.data, W.stride, W.rows, xi.data(), 1, &e);
-        *E = (float)e;
+        *E = (real)e;
     }
     void calculate_E(Vector *E, const Matrix &W, const Matrix &x) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         throwErrorIf(W.rows != W.cols || x.cols != W.cols, "%s, Shape does not match.", __func__);
-        std::vector<MatRow> rows = mat_rows(x);
+        auto rows = mat_rows(x);
         std::vector<int8_t> xi = rows_to_int8(rows.data(), x.rows, x.cols, false, __func__);
         std::vector<double> e(x.rows);
         quboEnergies(W.data, W.stride, W.rows, xi.data(), x.rows, e.data());
-        E->resize(x.rows);
-        for (int i = 0; i < x.rows; ++i) E->data[i] = (float)e[i];
+        to_vector(E, e);
     }
-    void calculateHamiltonian(Vector *h, Matrix *J, float *c, const Matrix &W) override {
+    void calculateHamiltonian(Vector *h, Matrix *J, real *c, const Matrix &W) override {
         throwErrorIf(h == nullptr || J == nullptr || c == nullptr, "%s, null output.", __func__);
         throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
         const int N = W.rows;
         h->resize(N);
-        std::vector<float> Jd((size_t)N * N);
+        std::vector<real> Jd((size_t)N * N);
         hamiltonian(W.data, W.stride, N, h->data, Jd.data(), c);
         J->resize(N, N);
-        for (int i = 0; i < N; ++i) memcpy(J->data + (size_t)i * J->stride, Jd.data() + (size_t)i * N, sizeof(float) * N);
+        for (int i = 0; i < N; ++i) memcpy(J->data + (size_t)i * J->stride, Jd.data() + (size_t)i * N, sizeof(real) * N);
     }
-    void calculate_E(float *E, const Vector &h, const Matrix &J, float c, const Vector &q) override {
+    void calculate_E(real *E, const Vector &h, const Matrix &J, real c, const Vector &q) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         throwErrorIf(J.rows != J.cols || h.size != J.cols || q.size != J.cols, "%s, Shape does not match.", __func__);
-        VecRow r{&q};
+        VecRow<real> r{&q};
         std::vector<int8_t> qi = rows_to_int8(&r, 1, q.size, true, __func__);
         double e;
         isingEnergies(h.data, J.data, J.stride, c, J.rows, qi.data(), 1, &e);
-        *E = (float)e;
+        *E = (real)e;
     }
-    void calculate_E(Vector *E, const Vector &h, const Matrix &J, float c, const Matrix &q) override {
+    void calculate_E(Vector *E, const Vector &h, const Matrix &J, real c, const Matrix &q) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         throwErrorIf(J.rows != J.cols || h.size != J.cols || q.cols != J.cols, "%s, Shape does not match.", __func__);
-        std::vector<MatRow> rows = mat_rows(q);
+        auto rows = mat_rows(q);
         std::vector<int8_t> qi = rows_to_int8(rows.data(), q.rows, q.cols, true, __func__);
         std::vector<double> e(q.rows);
         isingEnergies(h.data, J.data, J.stride, c, J.rows, qi.data(), q.rows, e.data());
-        E->resize(q.rows);
-        for (int i = 0; i < q.rows; ++i) E->data[i] = (float)e[i];
+        to_vector(E, e);
     }
 
 private:
@@ -1707,50 +1729,55 @@ private:
     }
 
     // sign * (-c - h q^T - q J q^T) of every row, h = 0 when null
-    void energies(const float *J, int ldJ, const float *h, double c, int N, const int8_t *q, int m, bool maximize,
+    void energies(const real *J, int ldJ, const real *h, double c, int N, const int8_t *q, int m, bool maximize,
                   double *E) {
         cudaStream_t s = st_.get();
         dJ_.ensure((size_t)N * N);
         dh_.ensure(N);
         dc64_.ensure(1);
-        SQ_CHECK(cudaMemcpy2DAsync(dJ_.p, sizeof(float) * N, J, sizeof(float) * ldJ, sizeof(float) * N, N,
+        SQ_CHECK(cudaMemcpy2DAsync(dJ_.p, sizeof(real) * N, J, sizeof(real) * ldJ, sizeof(real) * N, N,
                                    cudaMemcpyHostToDevice, s));
         if (h)
-            SQ_CHECK(cudaMemcpyAsync(dh_.p, h, sizeof(float) * N, cudaMemcpyHostToDevice, s));
+            SQ_CHECK(cudaMemcpyAsync(dh_.p, h, sizeof(real) * N, cudaMemcpyHostToDevice, s));
         else
-            SQ_CHECK(cudaMemsetAsync(dh_.p, 0, sizeof(float) * N, s));
+            SQ_CHECK(cudaMemsetAsync(dh_.p, 0, sizeof(real) * N, s));
         SQ_CHECK(cudaMemcpyAsync(dc64_.p, &c, sizeof(double), cudaMemcpyHostToDevice, s));
         const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)m, kFormulaScratch / (size_t)N));
         dq_.ensure((size_t)chunk * N);
-        dr_.ensure((size_t)chunk * N);
+        if (!kF64) dr_.ensure((size_t)chunk * N);
         dE_.ensure(chunk);
         for (int r0 = 0; r0 < m; r0 += chunk) {
             const int rows = std::min(chunk, m - r0);
             SQ_CHECK(cudaMemcpyAsync(dq_.p, q + (size_t)r0 * N, (size_t)rows * N, cudaMemcpyHostToDevice, s));
-            SQ_CHECK(sq103_dense_energy(dJ_.p, N, dh_.p, dc64_.p, dq_.p, N, rows, maximize ? 1 : 0, dr_.p, dE_.p,
-                                        nullptr, s));
+            if constexpr (kF64)
+                SQ_CHECK(sq103_dense_energy64(dJ_.p, dh_.p, c, dq_.p, N, rows, maximize ? 1 : 0, dE_.p, s));
+            else
+                SQ_CHECK(sq103_dense_energy(dJ_.p, N, dh_.p, dc64_.p, dq_.p, N, rows, maximize ? 1 : 0, dr_.p,
+                                            dE_.p, nullptr, s));
             SQ_CHECK(cudaMemcpyAsync(E + r0, dE_.p, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
             st_.sync();  // the next chunk reuses the staging buffers
         }
     }
 
     Stream st_;
-    DevBuf<float> dW_, dh_, dJ_, dc_;
+    DevBuf<real> dW_, dh_, dJ_, dc_;
     DevBuf<double> dc64_, dscr_, dr_, dE_;
     DevBuf<int8_t> dq_;
 };
 
-class BipartiteFormulas : public sq::cuda::BipartiteGraphFormulas<float> {
+template <class real>
+class BipartiteFormulasT : public sq::cuda::BipartiteGraphFormulas<real> {
 public:
-    typedef sq::MatrixType<float> Matrix;
-    typedef sq::VectorType<float> Vector;
+    typedef sq::MatrixType<real> Matrix;
+    typedef sq::VectorType<real> Vector;
+    static constexpr bool kF64 = std::is_same<real, double>::value;
 
     void assignDevice(sq::cuda::Device &device) override {
         SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
     }
 
     // E[i] = b0 x0_i^T + b1 x1_i^T + x1_i W x0_i^T (W: N1 x N0, row stride N0)
-    void quboEnergies(const float *b0, const float *b1, const float *W, int N0, int N1, const int8_t *x0,
+    void quboEnergies(const real *b0, const real *b1, const real *W, int N0, int N1, const int8_t *x0,
                       const int8_t *x1, int m, double *E) {
         check_shape(N0, N1, m, __func__);
         check_values(x0, (size_t)m * N0, false, __func__);
@@ -1759,7 +1786,7 @@ public:
     }
 
     // E[i1 * m0 + i0] = the QUBO energy of (x0_i0, x1_i1)
-    void quboEnergies2d(const float *b0, const float *b1, const float *W, int N0, int N1, const int8_t *x0, int m0,
+    void quboEnergies2d(const real *b0, const real *b1, const real *W, int N0, int N1, const int8_t *x0, int m0,
                         const int8_t *x1, int m1, double *E) {
         check_shape(N0, N1, m0, __func__);
         check_shape(N0, N1, m1, __func__);
@@ -1785,7 +1812,7 @@ public:
     }
 
     // E[i] = -c - h0 q0_i^T - h1 q1_i^T - q1_i J q0_i^T
-    void isingEnergies(const float *h0, const float *h1, const float *J, float c, int N0, int N1, const int8_t *q0,
+    void isingEnergies(const real *h0, const real *h1, const real *J, real c, int N0, int N1, const int8_t *q0,
                        const int8_t *q1, int m, double *E) {
         check_shape(N0, N1, m, __func__);
         check_values(q0, (size_t)m * N0, true, __func__);
@@ -1793,8 +1820,8 @@ public:
         energies(h0, h1, J, (double)c, N0, N1, q0, q1, m, false, E);
     }
 
-    void hamiltonian(const float *b0, const float *b1, const float *W, int N0, int N1, float *h0, float *h1,
-                     float *J, float *c) {
+    void hamiltonian(const real *b0, const real *b1, const real *W, int N0, int N1, real *h0, real *h1, real *J,
+                     real *c) {
         check_shape(N0, N1, 1, __func__);
         cudaStream_t s = st_.get();
         upload_problem(b0, b1, W, N0, N1);
@@ -1803,29 +1830,33 @@ public:
         dh1o_.ensure(N1);
         dc_.ensure(1);
         dc64_.ensure(1);
-        dscr_.ensure((size_t)N0 + N1);
-        SQ_CHECK(sq103_bipartite_hamiltonian(dh0_.p, dh1_.p, dJ_.p, N0, N1, 0, dh0o_.p, dh1o_.p, dJ2_.p, dc_.p,
-                                             dc64_.p, dscr_.p, s));
-        SQ_CHECK(cudaMemcpyAsync(h0, dh0o_.p, sizeof(float) * N0, cudaMemcpyDeviceToHost, s));
-        SQ_CHECK(cudaMemcpyAsync(h1, dh1o_.p, sizeof(float) * N1, cudaMemcpyDeviceToHost, s));
-        SQ_CHECK(cudaMemcpyAsync(J, dJ2_.p, sizeof(float) * N0 * N1, cudaMemcpyDeviceToHost, s));
-        SQ_CHECK(cudaMemcpyAsync(c, dc_.p, sizeof(float), cudaMemcpyDeviceToHost, s));
+        dscr_.ensure((size_t)N0 + 2 * N1);
+        if constexpr (kF64)
+            SQ_CHECK(sq103_bipartite_hamiltonian64(dh0_.p, dh1_.p, dJ_.p, N0, N1, dh0o_.p, dh1o_.p, dJ2_.p, dc_.p,
+                                                   dscr_.p, s));
+        else
+            SQ_CHECK(sq103_bipartite_hamiltonian(dh0_.p, dh1_.p, dJ_.p, N0, N1, 0, dh0o_.p, dh1o_.p, dJ2_.p, dc_.p,
+                                                 dc64_.p, dscr_.p, s));
+        SQ_CHECK(cudaMemcpyAsync(h0, dh0o_.p, sizeof(real) * N0, cudaMemcpyDeviceToHost, s));
+        SQ_CHECK(cudaMemcpyAsync(h1, dh1o_.p, sizeof(real) * N1, cudaMemcpyDeviceToHost, s));
+        SQ_CHECK(cudaMemcpyAsync(J, dJ2_.p, sizeof(real) * N0 * N1, cudaMemcpyDeviceToHost, s));
+        SQ_CHECK(cudaMemcpyAsync(c, dc_.p, sizeof(real), cudaMemcpyDeviceToHost, s));
         st_.sync();
     }
 
     // ---- the reference's interface
-    void calculate_E(float *E, const Vector &b0, const Vector &b1, const Matrix &W, const Vector &x0,
+    void calculate_E(real *E, const Vector &b0, const Vector &b1, const Matrix &W, const Vector &x0,
                      const Vector &x1) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         check_problem(b0, b1, W, __func__);
         throwErrorIf(x0.size != b0.size || x1.size != b1.size, "%s, Shape does not match.", __func__);
-        VecRow r0{&x0}, r1{&x1};
+        VecRow<real> r0{&x0}, r1{&x1};
         std::vector<int8_t> a = rows_to_int8(&r0, 1, x0.size, false, __func__);
         std::vector<int8_t> b = rows_to_int8(&r1, 1, x1.size, false, __func__);
-        std::vector<float> Wd = dense(W);
+        std::vector<real> Wd = dense_copy(W);
         double e;
         quboEnergies(b0.data, b1.data, Wd.data(), b0.size, b1.size, a.data(), b.data(), 1, &e);
-        *E = (float)e;
+        *E = (real)e;
     }
     void calculate_E(Vector *E, const Vector &b0, const Vector &b1, const Matrix &W, const Matrix &x0,
                      const Matrix &x1) override {
@@ -1833,70 +1864,68 @@ public:
         check_problem(b0, b1, W, __func__);
         throwErrorIf(x0.cols != b0.size || x1.cols != b1.size, "%s, Shape does not match.", __func__);
         throwErrorIf(x0.rows != x1.rows, "%s, Different batch dims between x0 and x1.", __func__);
-        std::vector<MatRow> r0 = mat_rows(x0), r1 = mat_rows(x1);
+        auto r0 = mat_rows(x0), r1 = mat_rows(x1);
         std::vector<int8_t> a = rows_to_int8(r0.data(), x0.rows, x0.cols, false, __func__);
         std::vector<int8_t> b = rows_to_int8(r1.data(), x1.rows, x1.cols, false, __func__);
-        std::vector<float> Wd = dense(W);
+        std::vector<real> Wd = dense_copy(W);
         std::vector<double> e(x0.rows);
         quboEnergies(b0.data, b1.data, Wd.data(), b0.size, b1.size, a.data(), b.data(), x0.rows, e.data());
-        E->resize(x0.rows);
-        for (int i = 0; i < x0.rows; ++i) E->data[i] = (float)e[i];
+        to_vector(E, e);
     }
     void calculate_E_2d(Matrix *E, const Vector &b0, const Vector &b1, const Matrix &W, const Matrix &x0,
                         const Matrix &x1) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         check_problem(b0, b1, W, __func__);
         throwErrorIf(x0.cols != b0.size || x1.cols != b1.size, "%s, Shape does not match.", __func__);
-        std::vector<MatRow> r0 = mat_rows(x0), r1 = mat_rows(x1);
+        auto r0 = mat_rows(x0), r1 = mat_rows(x1);
         std::vector<int8_t> a = rows_to_int8(r0.data(), x0.rows, x0.cols, false, __func__);
         std::vector<int8_t> b = rows_to_int8(r1.data(), x1.rows, x1.cols, false, __func__);
-        std::vector<float> Wd = dense(W);
+        std::vector<real> Wd = dense_copy(W);
         std::vector<double> e((size_t)x0.rows * x1.rows);
         quboEnergies2d(b0.data, b1.data, Wd.data(), b0.size, b1.size, a.data(), x0.rows, b.data(), x1.rows, e.data());
         E->resize(x1.rows, x0.rows);
         for (int i1 = 0; i1 < x1.rows; ++i1)
             for (int i0 = 0; i0 < x0.rows; ++i0)
-                E->data[(size_t)i1 * E->stride + i0] = (float)e[(size_t)i1 * x0.rows + i0];
+                E->data[(size_t)i1 * E->stride + i0] = (real)e[(size_t)i1 * x0.rows + i0];
     }
-    void calculateHamiltonian(Vector *h0, Vector *h1, Matrix *J, float *c, const Vector &b0, const Vector &b1,
+    void calculateHamiltonian(Vector *h0, Vector *h1, Matrix *J, real *c, const Vector &b0, const Vector &b1,
                               const Matrix &W) override {
         throwErrorIf(h0 == nullptr || h1 == nullptr || J == nullptr || c == nullptr, "%s, null output.", __func__);
         check_problem(b0, b1, W, __func__);
         const int N0 = b0.size, N1 = b1.size;
-        std::vector<float> Wd = dense(W), Jd((size_t)N0 * N1);
+        std::vector<real> Wd = dense_copy(W), Jd((size_t)N0 * N1);
         h0->resize(N0);
         h1->resize(N1);
         hamiltonian(b0.data, b1.data, Wd.data(), N0, N1, h0->data, h1->data, Jd.data(), c);
         J->resize(N1, N0);
-        for (int i = 0; i < N1; ++i) memcpy(J->data + (size_t)i * J->stride, Jd.data() + (size_t)i * N0, sizeof(float) * N0);
+        for (int i = 0; i < N1; ++i) memcpy(J->data + (size_t)i * J->stride, Jd.data() + (size_t)i * N0, sizeof(real) * N0);
     }
-    void calculate_E(float *E, const Vector &h0, const Vector &h1, const Matrix &J, float c, const Vector &q0,
+    void calculate_E(real *E, const Vector &h0, const Vector &h1, const Matrix &J, real c, const Vector &q0,
                      const Vector &q1) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         check_problem(h0, h1, J, __func__);
         throwErrorIf(q0.size != h0.size || q1.size != h1.size, "%s, Shape does not match.", __func__);
-        VecRow r0{&q0}, r1{&q1};
+        VecRow<real> r0{&q0}, r1{&q1};
         std::vector<int8_t> a = rows_to_int8(&r0, 1, q0.size, true, __func__);
         std::vector<int8_t> b = rows_to_int8(&r1, 1, q1.size, true, __func__);
-        std::vector<float> Jd = dense(J);
+        std::vector<real> Jd = dense_copy(J);
         double e;
         isingEnergies(h0.data, h1.data, Jd.data(), c, h0.size, h1.size, a.data(), b.data(), 1, &e);
-        *E = (float)e;
+        *E = (real)e;
     }
-    void calculate_E(Vector *E, const Vector &h0, const Vector &h1, const Matrix &J, float c, const Matrix &q0,
+    void calculate_E(Vector *E, const Vector &h0, const Vector &h1, const Matrix &J, real c, const Matrix &q0,
                      const Matrix &q1) override {
         throwErrorIf(E == nullptr, "%s, E is null.", __func__);
         check_problem(h0, h1, J, __func__);
         throwErrorIf(q0.cols != h0.size || q1.cols != h1.size, "%s, Shape does not match.", __func__);
         throwErrorIf(q0.rows != q1.rows, "%s, Different batch dims between q0 and q1.", __func__);
-        std::vector<MatRow> r0 = mat_rows(q0), r1 = mat_rows(q1);
+        auto r0 = mat_rows(q0), r1 = mat_rows(q1);
         std::vector<int8_t> a = rows_to_int8(r0.data(), q0.rows, q0.cols, true, __func__);
         std::vector<int8_t> b = rows_to_int8(r1.data(), q1.rows, q1.cols, true, __func__);
-        std::vector<float> Jd = dense(J);
+        std::vector<real> Jd = dense_copy(J);
         std::vector<double> e(q0.rows);
         isingEnergies(h0.data, h1.data, Jd.data(), c, h0.size, h1.size, a.data(), b.data(), q0.rows, e.data());
-        E->resize(q0.rows);
-        for (int i = 0; i < q0.rows; ++i) E->data[i] = (float)e[i];
+        to_vector(E, e);
     }
 
 private:
@@ -1906,25 +1935,19 @@ private:
     static void check_problem(const Vector &v0, const Vector &v1, const Matrix &M, const char *fn) {
         throwErrorIf(M.rows != v1.size || M.cols != v0.size, "%s, Shape does not match.", fn);
     }
-    // a matrix with row stride cols
-    static std::vector<float> dense(const Matrix &M) {
-        std::vector<float> d((size_t)M.rows * M.cols);
-        for (int i = 0; i < M.rows; ++i) memcpy(d.data() + (size_t)i * M.cols, M.data + (size_t)i * M.stride, sizeof(float) * M.cols);
-        return d;
-    }
 
-    void upload_problem(const float *v0, const float *v1, const float *M, int N0, int N1) {
+    void upload_problem(const real *v0, const real *v1, const real *M, int N0, int N1) {
         cudaStream_t s = st_.get();
         dh0_.ensure(N0);
         dh1_.ensure(N1);
         dJ_.ensure((size_t)N0 * N1);
-        SQ_CHECK(cudaMemcpyAsync(dh0_.p, v0, sizeof(float) * N0, cudaMemcpyHostToDevice, s));
-        SQ_CHECK(cudaMemcpyAsync(dh1_.p, v1, sizeof(float) * N1, cudaMemcpyHostToDevice, s));
-        SQ_CHECK(cudaMemcpyAsync(dJ_.p, M, sizeof(float) * N0 * N1, cudaMemcpyHostToDevice, s));
+        SQ_CHECK(cudaMemcpyAsync(dh0_.p, v0, sizeof(real) * N0, cudaMemcpyHostToDevice, s));
+        SQ_CHECK(cudaMemcpyAsync(dh1_.p, v1, sizeof(real) * N1, cudaMemcpyHostToDevice, s));
+        SQ_CHECK(cudaMemcpyAsync(dJ_.p, M, sizeof(real) * N0 * N1, cudaMemcpyHostToDevice, s));
     }
 
     // sign * (-c - h0 q0^T - h1 q1^T - q1 J q0^T) of every pair of rows
-    void energies(const float *h0, const float *h1, const float *J, double c, int N0, int N1, const int8_t *q0,
+    void energies(const real *h0, const real *h1, const real *J, double c, int N0, int N1, const int8_t *q0,
                   const int8_t *q1, int m, bool maximize, double *E) {
         cudaStream_t s = st_.get();
         upload_problem(h0, h1, J, N0, N1);
@@ -1933,24 +1956,33 @@ private:
         const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)m, kFormulaScratch / (size_t)N1));
         dq0_.ensure((size_t)chunk * N0);
         dq1_.ensure((size_t)chunk * N1);
-        dr_.ensure((size_t)chunk * N1);
+        if (!kF64) dr_.ensure((size_t)chunk * N1);
         dE_.ensure(chunk);
         for (int r0 = 0; r0 < m; r0 += chunk) {
             const int rows = std::min(chunk, m - r0);
             SQ_CHECK(cudaMemcpyAsync(dq0_.p, q0 + (size_t)r0 * N0, (size_t)rows * N0, cudaMemcpyHostToDevice, s));
             SQ_CHECK(cudaMemcpyAsync(dq1_.p, q1 + (size_t)r0 * N1, (size_t)rows * N1, cudaMemcpyHostToDevice, s));
-            SQ_CHECK(sq103_bipartite_energy(dJ_.p, dh0_.p, dh1_.p, dc64_.p, dq0_.p, dq1_.p, N0, N1, rows,
-                                            maximize ? 1 : 0, dr_.p, dE_.p, nullptr, s));
+            if constexpr (kF64)
+                SQ_CHECK(sq103_bipartite_energy64(dJ_.p, dh0_.p, dh1_.p, c, dq0_.p, dq1_.p, N0, N1, rows,
+                                                  maximize ? 1 : 0, dE_.p, s));
+            else
+                SQ_CHECK(sq103_bipartite_energy(dJ_.p, dh0_.p, dh1_.p, dc64_.p, dq0_.p, dq1_.p, N0, N1, rows,
+                                                maximize ? 1 : 0, dr_.p, dE_.p, nullptr, s));
             SQ_CHECK(cudaMemcpyAsync(E + r0, dE_.p, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
             st_.sync();
         }
     }
 
     Stream st_;
-    DevBuf<float> dh0_, dh1_, dJ_, dJ2_, dh0o_, dh1o_, dc_;
+    DevBuf<real> dh0_, dh1_, dJ_, dJ2_, dh0o_, dh1o_, dc_;
     DevBuf<double> dc64_, dscr_, dr_, dE_;
     DevBuf<int8_t> dq0_, dq1_;
 };
+
+typedef DenseFormulasT<float> DenseFormulas;
+typedef DenseFormulasT<double> DenseFormulas64;
+typedef BipartiteFormulasT<float> BipartiteFormulas;
+typedef BipartiteFormulasT<double> BipartiteFormulas64;
 
 }  // namespace sq103
 
@@ -1981,6 +2013,14 @@ DenseGraphFormulas<float> *newDenseGraphFormulas<float>() {
 template <>
 BipartiteGraphFormulas<float> *newBipartiteGraphFormulas<float>() {
     return new sq103::BipartiteFormulas();
+}
+template <>
+DenseGraphFormulas<double> *newDenseGraphFormulas<double>() {
+    return new sq103::DenseFormulas64();
+}
+template <>
+BipartiteGraphFormulas<double> *newBipartiteGraphFormulas<double>() {
+    return new sq103::BipartiteFormulas64();
 }
 Device *newDevice(int devNo) { return new sq103::DeviceImpl(devNo); }
 

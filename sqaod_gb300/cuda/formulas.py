@@ -7,9 +7,11 @@ Each call goes through one sq103_{dg,bg}_formulas_* entry point of the C ABI,
 which uploads the arguments, runs the device kernels and copies the result
 back.  Energies are summed in FP64 on the device and returned in `dtype`.
 
+dtype numpy.float32 runs the fp32-input kernels the solvers use (FP64 sums),
+numpy.float64 plain FP64 kernels (the reference's <double> instantiation);
+other dtypes raise.
+
 Differences from the reference, all deliberate:
-  * only dtype=numpy.float32 is provided (other dtypes raise), as for the
-    solvers of this package;
   * bits must be 0 / 1 and spins -1 / +1 (the device kernels check);
   * bipartite_graph_batch_calculate_E_2d works for any two batch sizes and
     returns E[i1][i0]; the reference's version always raises (its body reads
@@ -21,10 +23,8 @@ import numpy as np
 
 from .. import common
 from .._lib import call, lib, ptr
-from .solvers import _check_dtype
 
 _c_int = ctypes.c_int
-_c_float = ctypes.c_float
 
 
 class _FormulaSet:
@@ -51,6 +51,25 @@ class _FormulaSet:
 
 
 _objs = {}
+
+
+def _check_dtype(dtype):
+    d = np.dtype(np.float32 if dtype is None else dtype)
+    if d not in (np.float32, np.float64):
+        raise RuntimeError("dtype %s is not provided: the formulas compute in float32 or float64." % d)
+    return d.type
+
+
+def _real(dtype):
+    return ctypes.c_double if dtype is np.float64 else ctypes.c_float
+
+
+def _dg(dtype):
+    return _obj('sq103_dg_formulas64' if dtype is np.float64 else 'sq103_dg_formulas')
+
+
+def _bg(dtype):
+    return _obj('sq103_bg_formulas64' if dtype is np.float64 else 'sq103_bg_formulas')
 
 
 def _obj(prefix):
@@ -136,7 +155,7 @@ def dense_graph_batch_calculate_E(W, x, dtype):
     W = common.symmetrize(W)
     x = _dense_rows(W, common.fix_type(x, np.int8), 'W, x')
     E = np.empty(x.shape[0], np.float64)
-    _obj('sq103_dg_formulas')('calculate_E', ptr(W), _c_int(W.shape[0]), ptr(x), _c_int(x.shape[0]), ptr(E))
+    _dg(dtype)('calculate_E', ptr(W), _c_int(W.shape[0]), ptr(x), _c_int(x.shape[0]), ptr(E))
     return E.astype(dtype)
 
 
@@ -150,7 +169,7 @@ def dense_graph_calculate_hamiltonian(W, dtype):
     h = np.empty(N, dtype)
     J = np.empty((N, N), dtype)
     c = np.empty(1, dtype)
-    _obj('sq103_dg_formulas')('calculate_hamiltonian', ptr(W), _c_int(N), ptr(h), ptr(J), ptr(c))
+    _dg(dtype)('calculate_hamiltonian', ptr(W), _c_int(N), ptr(h), ptr(J), ptr(c))
     return h, J, c[0]
 
 
@@ -171,8 +190,8 @@ def dense_graph_batch_calculate_E_from_spin(h, J, c, q, dtype):
         _dims('h, J', h, J)
     q = _dense_rows(J, q, 'J, q')
     E = np.empty(q.shape[0], np.float64)
-    _obj('sq103_dg_formulas')('calculate_E_from_spin', ptr(h), ptr(J), _c_float(float(c)), _c_int(J.shape[0]),
-                              ptr(q), _c_int(q.shape[0]), ptr(E))
+    _dg(dtype)('calculate_E_from_spin', ptr(h), ptr(J), _real(dtype)(float(c)), _c_int(J.shape[0]),
+               ptr(q), _c_int(q.shape[0]), ptr(E))
     return E.astype(dtype)
 
 
@@ -191,8 +210,8 @@ def bipartite_graph_batch_calculate_E(b0, b1, W, x0, x1, dtype):
     _bipartite_problem(b0, b1, W, ('b0', 'b1', 'W'))
     x0, x1 = _bipartite_rows(W, x0, x1, 'x0, x1')
     E = np.empty(x0.shape[0], np.float64)
-    _obj('sq103_bg_formulas')('calculate_E', ptr(b0), ptr(b1), ptr(W), _c_int(W.shape[1]), _c_int(W.shape[0]),
-                              ptr(x0), ptr(x1), _c_int(x0.shape[0]), ptr(E))
+    _bg(dtype)('calculate_E', ptr(b0), ptr(b1), ptr(W), _c_int(W.shape[1]), _c_int(W.shape[0]),
+               ptr(x0), ptr(x1), _c_int(x0.shape[0]), ptr(E))
     return E.astype(dtype)
 
 
@@ -205,8 +224,8 @@ def bipartite_graph_batch_calculate_E_2d(b0, b1, W, x0, x1, dtype):
     x0, x1 = _bipartite_rows(W, x0, x1, 'x0, x1', same_batch=False)
     m0, m1 = x0.shape[0], x1.shape[0]
     E = np.empty((m1, m0), np.float64)
-    _obj('sq103_bg_formulas')('calculate_E_2d', ptr(b0), ptr(b1), ptr(W), _c_int(W.shape[1]), _c_int(W.shape[0]),
-                              ptr(x0), _c_int(m0), ptr(x1), _c_int(m1), ptr(E))
+    _bg(dtype)('calculate_E_2d', ptr(b0), ptr(b1), ptr(W), _c_int(W.shape[1]), _c_int(W.shape[0]),
+               ptr(x0), _c_int(m0), ptr(x1), _c_int(m1), ptr(E))
     return E.astype(dtype)
 
 
@@ -220,8 +239,8 @@ def bipartite_graph_calculate_hamiltonian(b0, b1, W, dtype):
     h1 = np.empty(N1, dtype)
     J = np.empty((N1, N0), dtype)
     c = np.empty(1, dtype)
-    _obj('sq103_bg_formulas')('calculate_hamiltonian', ptr(b0), ptr(b1), ptr(W), _c_int(N0), _c_int(N1), ptr(h0),
-                              ptr(h1), ptr(J), ptr(c))
+    _bg(dtype)('calculate_hamiltonian', ptr(b0), ptr(b1), ptr(W), _c_int(N0), _c_int(N1), ptr(h0),
+               ptr(h1), ptr(J), ptr(c))
     return h0, h1, J, c[0]
 
 
@@ -240,7 +259,7 @@ def bipartite_graph_batch_calculate_E_from_spin(h0, h1, J, c, q0, q1, dtype):
     _scalar('c', c)
     q0, q1 = _bipartite_rows(J, q0, q1, 'q0, q1')
     E = np.empty(q0.shape[0], np.float64)
-    _obj('sq103_bg_formulas')('calculate_E_from_spin', ptr(h0), ptr(h1), ptr(J), _c_float(float(c)),
-                              _c_int(J.shape[1]), _c_int(J.shape[0]), ptr(q0), ptr(q1), _c_int(q0.shape[0]),
-                              ptr(E))
+    _bg(dtype)('calculate_E_from_spin', ptr(h0), ptr(h1), ptr(J), _real(dtype)(float(c)),
+               _c_int(J.shape[1]), _c_int(J.shape[0]), ptr(q0), ptr(q1), _c_int(q0.shape[0]),
+               ptr(E))
     return E.astype(dtype)

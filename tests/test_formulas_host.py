@@ -8,13 +8,13 @@ import sqaod_gb300 as sq
 F32 = np.float32
 
 
-def test_float64_is_not_provided():
+def test_only_float32_and_float64_are_provided():
     W = np.eye(4)
-    with pytest.raises(RuntimeError, match="float32 only"):
-        sq.cuda.formulas.dense_graph_calculate_E(W, np.zeros(4, np.int8), np.float64)
-    with pytest.raises(RuntimeError, match="float32 only"):
+    with pytest.raises(RuntimeError, match="float32 or float64"):
+        sq.cuda.formulas.dense_graph_calculate_E(W, np.zeros(4, np.int8), np.float16)
+    with pytest.raises(RuntimeError, match="float32 or float64"):
         sq.cuda.formulas.bipartite_graph_calculate_hamiltonian(np.zeros(2), np.zeros(3), np.zeros((3, 2)),
-                                                              np.float64)
+                                                              np.int32)
 
 
 def test_shape_and_type_checks():
