@@ -16,6 +16,7 @@
 // Bipartite: E(x0, x1) = b0.x0 + b1.x1 + x1^T W x0 (sqaodc/cpu/SharedFormulas.cpp:123-144).
 // One CTA per x1 value; D[j] = b0[j] + sum_{i in x1} W[i][j]; E is the sum of
 // 7-bit-group lookups over x0 plus b1.x1.
+#include <cstdint>
 #include <cstring>
 
 #include "sq_common.cuh"
@@ -123,14 +124,53 @@ __global__ void __launch_bounds__(kBfThreads) bf_dense_pass(const float *W, int 
         uint32_t loE = (uint32_t)min((uint64_t)1 << L, xe - x0);
         float lmin = __int_as_float(0x7f800000);
         const uint32_t mask = (1u << Ll) - 1u;
-        for (uint32_t lo = loB + threadIdx.x; lo < loE; lo += blockDim.x) {
-            float e = (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]);
+        auto visit = [&](uint32_t lo, float e) {
             if (PASS == 0) {
                 lmin = fminf(lmin, e);
             } else if (e <= thr) {
                 int slot = atomicAdd(&ws->count, 1);
                 if (slot < cap) cand[slot] = x0 | lo;
             }
+        };
+        // four consecutive states per thread: one 16-byte load of the E_ll table and one
+        // tabHi lookup for the four; a thread's tabLo entries stay the same across its
+        // iterations (the stride 4 * blockDim.x is a multiple of 2^Ll), so they are
+        // kept in registers.  Every energy is summed in the same order as one at a time.
+        const uint32_t vb = (loB + 3u) & ~3u, ve = loE & ~3u;
+        const uint32_t step4 = 4u * blockDim.x;
+        if (vb < ve && (step4 & mask) == 0 && !(reinterpret_cast<uintptr_t>(ws->ell) & 15)) {
+            for (uint32_t lo = loB + threadIdx.x; lo < vb; lo += blockDim.x)
+                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
+            for (uint32_t lo = ve + threadIdx.x; lo < loE; lo += blockDim.x)
+                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
+            const uint32_t first = vb + 4u * threadIdx.x;
+            const float t0 = tabLo[first & mask], t1 = tabLo[(first + 1u) & mask];
+            const float t2 = tabLo[(first + 2u) & mask], t3 = tabLo[(first + 3u) & mask];
+            uint32_t lo = first;
+            for (; lo + step4 < ve; lo += 2u * step4) {
+                const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
+                const float4 k = *reinterpret_cast<const float4 *>(&ws->ell[lo + step4]);
+                const float th = tabHi[lo >> Ll], tk = tabHi[(lo + step4) >> Ll];
+                visit(lo, (base + l.x) + (th + t0));
+                visit(lo + 1u, (base + l.y) + (th + t1));
+                visit(lo + 2u, (base + l.z) + (th + t2));
+                visit(lo + 3u, (base + l.w) + (th + t3));
+                visit(lo + step4, (base + k.x) + (tk + t0));
+                visit(lo + step4 + 1u, (base + k.y) + (tk + t1));
+                visit(lo + step4 + 2u, (base + k.z) + (tk + t2));
+                visit(lo + step4 + 3u, (base + k.w) + (tk + t3));
+            }
+            for (; lo < ve; lo += step4) {
+                const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
+                const float th = tabHi[lo >> Ll];
+                visit(lo, (base + l.x) + (th + t0));
+                visit(lo + 1u, (base + l.y) + (th + t1));
+                visit(lo + 2u, (base + l.z) + (th + t2));
+                visit(lo + 3u, (base + l.w) + (th + t3));
+            }
+        } else {
+            for (uint32_t lo = loB + threadIdx.x; lo < loE; lo += blockDim.x)
+                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
         }
         if (PASS == 0) {
             for (int o = 16; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
