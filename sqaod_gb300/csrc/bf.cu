@@ -62,115 +62,128 @@ __global__ void bf_lo_table(const float *W, int N, int L, BfWorkspace *ws) {
     ws->ell[lo] = (float)e;
 }
 
-// per-CTA setup for one hi value: base = E_hh(hi); tabHi / tabLo = cross term halves
-__device__ void bf_block_setup(const float *W, int N, int L, uint64_t hi, float *base, float *tabHi,
-                               float *tabLo, float *C, int Lh, int Ll) {
-    int H = N - L;
-    int tid = threadIdx.x;
-    // C[b] = 2 sum_{i in hi set} W[i][N-1-b]; hi bit c <-> variable H-1-c
-    if (tid < L) {
-        double s = 0.;
-        for (int c = 0; c < H; ++c)
-            if ((hi >> c) & 1ull) s += (double)W[(size_t)(H - 1 - c) * N + (N - 1 - tid)];
-        C[tid] = (float)(2. * s);
-    }
-    if (tid >= 32 && tid < 64) {
-        // E_hh(hi): the second warp sums the selected rows (one per lane, FP64) and
-        // reduces them in a fixed tree order
-        double e = 0.;
-        for (int c = tid - 32; c < H; c += 32) {
-            if (!((hi >> c) & 1ull)) continue;
-            const float *row = W + (size_t)(H - 1 - c) * N;
-            for (int d = 0; d < H; ++d)
-                if ((hi >> d) & 1ull) e += (double)row[H - 1 - d];
+// per-CTA set-up for the K consecutive hi values hi0 .. hi0 + K - 1 that are <= he:
+// each hi value's set-up (C_hi, E_hh) runs in its own group of kBfThreads / K
+// threads, all at once: base = E_hh(hi), C_hi, and the cross-term half tables
+template <int K>
+__device__ void bf_block_setup_k(const float *W, int N, int L, uint64_t hi0, uint64_t he, float *base,
+                                 float (*tabHi)[128], float (*tabLo)[128], float (*C)[kLoBits], int Lh, int Ll) {
+    static_assert(kBfThreads / K >= 64 && kBfThreads % K == 0, "a group needs two warps");
+    constexpr int kGroup = kBfThreads / K;
+    const int H = N - L;
+    const int tid = threadIdx.x, g = tid / kGroup, t = tid % kGroup;
+    const uint64_t hi = hi0 + g;
+    if (hi <= he) {
+        if (t < L) {
+            double s = 0.;
+            for (int c = 0; c < H; ++c)
+                if ((hi >> c) & 1ull) s += (double)W[(size_t)(H - 1 - c) * N + (N - 1 - t)];
+            C[g][t] = (float)(2. * s);
         }
-        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
-        if (tid == 32) *base = (float)e;
+        if (t >= 32 && t < 64) {
+            double e = 0.;
+            for (int c = t - 32; c < H; c += 32) {
+                if (!((hi >> c) & 1ull)) continue;
+                const float *row = W + (size_t)(H - 1 - c) * N;
+                for (int d = 0; d < H; ++d)
+                    if ((hi >> d) & 1ull) e += (double)row[H - 1 - d];
+            }
+            for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+            if (t == 32) base[g] = (float)e;
+        }
     }
     __syncthreads();
-    // tables over the two halves of lo: lo = (a << Ll) | b
-    for (int t = tid; t < (1 << Lh); t += blockDim.x) {
+    for (int idx = tid; idx < (K << Lh); idx += blockDim.x) {
+        const int k = idx >> Lh, u = idx & ((1 << Lh) - 1);
         float s = 0.f;
-        for (int k = 0; k < Lh; ++k)
-            if ((t >> k) & 1) s += C[Ll + k];
-        tabHi[t] = s;
+        for (int b = 0; b < Lh; ++b)
+            if ((u >> b) & 1) s += C[k][Ll + b];
+        tabHi[k][u] = s;
     }
-    for (int t = tid; t < (1 << Ll); t += blockDim.x) {
+    for (int idx = tid; idx < (K << Ll); idx += blockDim.x) {
+        const int k = idx >> Ll, u = idx & ((1 << Ll) - 1);
         float s = 0.f;
-        for (int k = 0; k < Ll; ++k)
-            if ((t >> k) & 1) s += C[k];
-        tabLo[t] = s;
+        for (int b = 0; b < Ll; ++b)
+            if ((u >> b) & 1) s += C[k][b];
+        tabLo[k][u] = s;
     }
     __syncthreads();
 }
 
-// PASS 0: minimum; PASS 1: collect x with E <= thr
+// PASS 0: minimum; PASS 1: collect x with E <= thr.  A CTA takes kBfHiPerRound hi
+// values per round of set-up.
+constexpr int kBfHiPerRound = 4;
 template <int PASS>
 __global__ void __launch_bounds__(kBfThreads) bf_dense_pass(const float *W, int N, int L, uint64_t xb, uint64_t xe,
                                                             float slack, BfWorkspace *ws, uint64_t *cand, int cap) {
-    __shared__ float tabHi[128], tabLo[128], C[kLoBits];
-    __shared__ float base;
+    constexpr int K = kBfHiPerRound;
+    __shared__ float tabHi[K][128], tabLo[K][128], C[K][kLoBits];
+    __shared__ float base[K];
     __shared__ unsigned int blockMin;
     const int Lh = L / 2, Ll = L - Lh;
     const uint64_t hb = xb >> L, he = (xe - 1) >> L;
     float thr = 0.f;
     if (PASS == 1) thr = dec_float(ws->minEnc) + slack;
-    for (uint64_t hi = hb + blockIdx.x; hi <= he; hi += gridDim.x) {
-        bf_block_setup(W, N, L, hi, &base, tabHi, tabLo, C, Lh, Ll);
+    const uint32_t mask = (1u << Ll) - 1u;
+    for (uint64_t hi0 = hb + (uint64_t)blockIdx.x * K; hi0 <= he; hi0 += (uint64_t)gridDim.x * K) {
+        bf_block_setup_k<K>(W, N, L, hi0, he, base, tabHi, tabLo, C, Lh, Ll);
         if (PASS == 0 && threadIdx.x == 0) blockMin = 0xffffffffu;
         __syncthreads();
-        uint64_t x0 = hi << L;
-        uint32_t loB = (uint32_t)(xb > x0 ? xb - x0 : 0);
-        uint32_t loE = (uint32_t)min((uint64_t)1 << L, xe - x0);
         float lmin = __int_as_float(0x7f800000);
-        const uint32_t mask = (1u << Ll) - 1u;
-        auto visit = [&](uint32_t lo, float e) {
-            if (PASS == 0) {
-                lmin = fminf(lmin, e);
-            } else if (e <= thr) {
-                int slot = atomicAdd(&ws->count, 1);
-                if (slot < cap) cand[slot] = x0 | lo;
+        for (int k = 0; k < K && hi0 + k <= he; ++k) {
+            const float bk = base[k];
+            const float *tH = tabHi[k], *tL = tabLo[k];
+            const uint64_t x0 = (hi0 + k) << L;
+            const uint32_t loB = (uint32_t)(xb > x0 ? xb - x0 : 0);
+            const uint32_t loE = (uint32_t)min((uint64_t)1 << L, xe - x0);
+            auto visit = [&](uint32_t lo, float e) {
+                if (PASS == 0) {
+                    lmin = fminf(lmin, e);
+                } else if (e <= thr) {
+                    int slot = atomicAdd(&ws->count, 1);
+                    if (slot < cap) cand[slot] = x0 | lo;
+                }
+            };
+            // four consecutive states per thread: one 16-byte load of the E_ll table and one
+            // tabHi lookup for the four; a thread's tabLo entries stay the same across its
+            // iterations (the stride 4 * blockDim.x is a multiple of 2^Ll), so they are
+            // kept in registers.  Every energy is summed in the same order as one at a time.
+            const uint32_t vb = (loB + 3u) & ~3u, ve = loE & ~3u;
+            const uint32_t step4 = 4u * blockDim.x;
+            if (vb < ve && (step4 & mask) == 0 && !(reinterpret_cast<uintptr_t>(ws->ell) & 15)) {
+                for (uint32_t lo = loB + threadIdx.x; lo < vb; lo += blockDim.x)
+                    visit(lo, (bk + ws->ell[lo]) + (tH[lo >> Ll] + tL[lo & mask]));
+                for (uint32_t lo = ve + threadIdx.x; lo < loE; lo += blockDim.x)
+                    visit(lo, (bk + ws->ell[lo]) + (tH[lo >> Ll] + tL[lo & mask]));
+                const uint32_t first = vb + 4u * threadIdx.x;
+                const float t0 = tL[first & mask], t1 = tL[(first + 1u) & mask];
+                const float t2 = tL[(first + 2u) & mask], t3 = tL[(first + 3u) & mask];
+                uint32_t lo = first;
+                for (; lo + step4 < ve; lo += 2u * step4) {
+                    const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
+                    const float4 q = *reinterpret_cast<const float4 *>(&ws->ell[lo + step4]);
+                    const float th = tH[lo >> Ll], tq = tH[(lo + step4) >> Ll];
+                    visit(lo, (bk + l.x) + (th + t0));
+                    visit(lo + 1u, (bk + l.y) + (th + t1));
+                    visit(lo + 2u, (bk + l.z) + (th + t2));
+                    visit(lo + 3u, (bk + l.w) + (th + t3));
+                    visit(lo + step4, (bk + q.x) + (tq + t0));
+                    visit(lo + step4 + 1u, (bk + q.y) + (tq + t1));
+                    visit(lo + step4 + 2u, (bk + q.z) + (tq + t2));
+                    visit(lo + step4 + 3u, (bk + q.w) + (tq + t3));
+                }
+                for (; lo < ve; lo += step4) {
+                    const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
+                    const float th = tH[lo >> Ll];  // the four share lo >> Ll (2^Ll is a multiple of 4)
+                    visit(lo, (bk + l.x) + (th + t0));
+                    visit(lo + 1u, (bk + l.y) + (th + t1));
+                    visit(lo + 2u, (bk + l.z) + (th + t2));
+                    visit(lo + 3u, (bk + l.w) + (th + t3));
+                }
+            } else {
+                for (uint32_t lo = loB + threadIdx.x; lo < loE; lo += blockDim.x)
+                    visit(lo, (bk + ws->ell[lo]) + (tH[lo >> Ll] + tL[lo & mask]));
             }
-        };
-        // four consecutive states per thread: one 16-byte load of the E_ll table and one
-        // tabHi lookup for the four; a thread's tabLo entries stay the same across its
-        // iterations (the stride 4 * blockDim.x is a multiple of 2^Ll), so they are
-        // kept in registers.  Every energy is summed in the same order as one at a time.
-        const uint32_t vb = (loB + 3u) & ~3u, ve = loE & ~3u;
-        const uint32_t step4 = 4u * blockDim.x;
-        if (vb < ve && (step4 & mask) == 0 && !(reinterpret_cast<uintptr_t>(ws->ell) & 15)) {
-            for (uint32_t lo = loB + threadIdx.x; lo < vb; lo += blockDim.x)
-                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
-            for (uint32_t lo = ve + threadIdx.x; lo < loE; lo += blockDim.x)
-                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
-            const uint32_t first = vb + 4u * threadIdx.x;
-            const float t0 = tabLo[first & mask], t1 = tabLo[(first + 1u) & mask];
-            const float t2 = tabLo[(first + 2u) & mask], t3 = tabLo[(first + 3u) & mask];
-            uint32_t lo = first;
-            for (; lo + step4 < ve; lo += 2u * step4) {
-                const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
-                const float4 k = *reinterpret_cast<const float4 *>(&ws->ell[lo + step4]);
-                const float th = tabHi[lo >> Ll], tk = tabHi[(lo + step4) >> Ll];
-                visit(lo, (base + l.x) + (th + t0));
-                visit(lo + 1u, (base + l.y) + (th + t1));
-                visit(lo + 2u, (base + l.z) + (th + t2));
-                visit(lo + 3u, (base + l.w) + (th + t3));
-                visit(lo + step4, (base + k.x) + (tk + t0));
-                visit(lo + step4 + 1u, (base + k.y) + (tk + t1));
-                visit(lo + step4 + 2u, (base + k.z) + (tk + t2));
-                visit(lo + step4 + 3u, (base + k.w) + (tk + t3));
-            }
-            for (; lo < ve; lo += step4) {
-                const float4 l = *reinterpret_cast<const float4 *>(&ws->ell[lo]);
-                const float th = tabHi[lo >> Ll];
-                visit(lo, (base + l.x) + (th + t0));
-                visit(lo + 1u, (base + l.y) + (th + t1));
-                visit(lo + 2u, (base + l.z) + (th + t2));
-                visit(lo + 3u, (base + l.w) + (th + t3));
-            }
-        } else {
-            for (uint32_t lo = loB + threadIdx.x; lo < loE; lo += blockDim.x)
-                visit(lo, (base + ws->ell[lo]) + (tabHi[lo >> Ll] + tabLo[lo & mask]));
         }
         if (PASS == 0) {
             for (int o = 16; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
@@ -308,7 +321,7 @@ SQ103_API int sq103_dense_bf_range(const float *W, int N, uint64_t xBegin, uint6
     bf_init_ws<<<1, 1, 0, s>>>(w);
     bf_lo_table<<<((1 << L) + 255) / 256, 256, 0, s>>>(W, N, L, w);
     uint64_t nHi = ((xEnd - 1) >> L) - (xBegin >> L) + 1;
-    int grid = bf_grid(nHi);
+    int grid = bf_grid((nHi + kBfHiPerRound - 1) / kBfHiPerRound);
     bf_dense_pass<0><<<grid, kBfThreads, 0, s>>>(W, N, L, xBegin, xEnd, slack, w, cand, cap);
     bf_dense_pass<1><<<grid, kBfThreads, 0, s>>>(W, N, L, xBegin, xEnd, slack, w, cand, cap);
     unsigned int enc = 0;
