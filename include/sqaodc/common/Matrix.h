@@ -46,7 +46,7 @@ struct MatrixType {
     void allocate(SizeType r, SizeType c) {
         free();
         rows = r; cols = c; stride = c; mapped = false;
-        data = (r * c) ? new V[(size_t)r * c]() : nullptr;
+        data = (r > 0 && c > 0) ? new V[(size_t)r * c]() : nullptr;
     }
     void resize(SizeType r, SizeType c) {
         if (r != rows || c != cols || mapped) allocate(r, c);

@@ -132,3 +132,46 @@ def test_generators_match_reference_draws(golden):
     W = sq.generate_random_symmetric_W(16)
     assert np.allclose(np.rint(W * 16384) / 16384., golden["dg_r16_W"])
     assert np.array_equal(sq.create_bitset_sequence([5], 4), np.array([[0, 1, 0, 1]], np.int8))
+
+
+def test_cpp_headers_compile(tmp_path):
+    """A C++ caller written against the reference's API compiles against include/
+    (factories, solver and formula interfaces, deleteInstance)."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "caller.cpp"
+    src.write_text(r'''
+#include <sqaodc/sqaodc.h>
+namespace sq = sqaod;
+void use() {
+    sq::cuda::DenseGraphAnnealer<float> *a = sq::cuda::newDenseGraphAnnealer<float>();
+    sq::MatrixType<float> W(4, 4);
+    a->setQUBO(W, sq::optMinimize);
+    a->setPreference(sq::Preference(sq::pnNumTrotters, 8));
+    a->prepare();
+    a->randomizeSpin();
+    a->annealOneStep(1.f, 10.f);
+    a->makeSolution();
+    const sq::VectorType<float> &E = a->get_E();
+    (void)E;
+    sq::deleteInstance(a);
+    sq::cuda::DenseGraphFormulas<double> *f = sq::cuda::newDenseGraphFormulas<double>();
+    sq::MatrixType<double> Wd(4, 4);
+    sq::VectorType<double> x(4), h;
+    sq::MatrixType<double> J;
+    double e = 0., c = 0.;
+    f->calculate_E(&e, Wd, x);
+    f->calculateHamiltonian(&h, &J, &c, Wd);
+    sq::deleteInstance(f);
+    sq::cuda::BipartiteGraphFormulas<float> *g = sq::cuda::newBipartiteGraphFormulas<float>();
+    sq::deleteInstance(g);
+}
+''')
+    import os
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", inc, "-c", str(src), "-o", str(tmp_path / "caller.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
