@@ -117,7 +117,7 @@ def test_dense_energy_vs_fp64_large(sq, orc):
     a.randomize_spin()
     q = np.array(a.get_q())
     h, J, c = orc.dg_hamiltonian(W)
-    # spec criterion: within 1e-5 of the all-FP64 oracle
+    # the precision criterion: within 1e-5 relative of the all-FP64 oracle
     assert rel_close(a.get_E(), orc.dg_energy_ising(h, J, c, q))
     # the FP64 evaluation itself: exact up to rounding, given the fp32 h and J the API stores
     h32, J32, _ = a.get_hamiltonian()
