@@ -23,7 +23,8 @@ def _check_dtype(dtype):
     if dtype is None:
         return np.float32
     if np.dtype(dtype) != np.float32:
-        raise RuntimeError("dtype %s is not provided: this build computes in float32 only." % np.dtype(dtype))
+        raise RuntimeError("dtype %s is not provided: the solvers compute in float32 only "
+                           "(the formulas also in float64)." % np.dtype(dtype))
     return np.float32
 
 
