@@ -9,6 +9,9 @@ F32 = np.float32
 
 
 def test_only_float32_and_float64_are_provided():
+    # sqaodpy/tests/test_wrong_type.py: an integer dtype raises RuntimeError
+    with pytest.raises(RuntimeError):
+        sq.cuda.formulas.dense_graph_calculate_hamiltonian(np.ones((4, 4), np.int32), np.int32)
     W = np.eye(4)
     with pytest.raises(RuntimeError, match="float32 or float64"):
         sq.cuda.formulas.dense_graph_calculate_E(W, np.zeros(4, np.int8), np.float16)

@@ -93,7 +93,13 @@ def test_dense_triangular_W_is_symmetrized():
     W = sym_W(40, 2)
     U = np.triu(W) + np.triu(W, 1)  # upper triangle carrying W_ij + W_ji
     x = (np.random.default_rng(3).random((16, 40)) < 0.5).astype(np.int8)
-    assert np.array_equal(f.dense_graph_batch_calculate_E(U, x, F32), f.dense_graph_batch_calculate_E(W, x, F32))
+    E = f.dense_graph_batch_calculate_E(W, x, F32)
+    assert np.array_equal(f.dense_graph_batch_calculate_E(U, x, F32), E)
+    assert np.array_equal(f.dense_graph_batch_calculate_E(U.T.copy(), x, F32), E)  # lower triangle
+    h, J, c = f.dense_graph_calculate_hamiltonian(W, F32)
+    for T in (U, U.T.copy()):  # sqaodpy/tests/test_symmetrize_formulas.py
+        hT, JT, cT = f.dense_graph_calculate_hamiltonian(T, F32)
+        assert np.array_equal(hT, h) and np.array_equal(JT, J) and cT == c
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
