@@ -237,9 +237,7 @@ __global__ void __launch_bounds__(kBfThreads) bf_bip_pass(const float *b0, const
         }
         __syncthreads();
         float lmin = __int_as_float(0x7f800000);
-        for (uint64_t x0 = x0b + tid; x0 < x0e; x0 += blockDim.x) {
-            float e = base;
-            for (int g = 0; g < nG; ++g) e += tab[g][(x0 >> (7 * g)) & 127];
+        auto visit = [&](uint64_t x0, float e) {
             if (PASS == 0) {
                 lmin = fminf(lmin, e);
             } else if (e <= thr) {
@@ -249,6 +247,40 @@ __global__ void __launch_bounds__(kBfThreads) bf_bip_pass(const float *b0, const
                     cand[2 * slot + 1] = x1;
                 }
             }
+        };
+        auto energy = [&](uint64_t x0) {
+            float e = base;
+            for (int g = 0; g < nG; ++g) e += tab[g][(x0 >> (7 * g)) & 127];
+            return e;
+        };
+        // four consecutive x0 per thread: their first-group entries stay the same across
+        // the thread's iterations (the stride 4 * blockDim.x is a multiple of 128), so
+        // they are kept in registers, and the four share every higher group's lookup.
+        // Each energy adds its groups in the same order as one at a time.
+        const uint64_t vb = (x0b + 3) & ~3ull, ve = x0e & ~3ull;
+        const uint32_t step4 = 4u * blockDim.x;
+        if (nG >= 2 && vb < ve && (step4 & 127u) == 0) {
+            for (uint64_t x0 = x0b + tid; x0 < vb && x0 < x0e; x0 += blockDim.x) visit(x0, energy(x0));
+            for (uint64_t x0 = ve + tid; x0 < x0e; x0 += blockDim.x) visit(x0, energy(x0));
+            const uint64_t first = vb + 4u * tid;
+            const float t0 = base + tab[0][first & 127], t1 = base + tab[0][(first + 1) & 127];
+            const float t2 = base + tab[0][(first + 2) & 127], t3 = base + tab[0][(first + 3) & 127];
+            for (uint64_t x0 = first; x0 < ve; x0 += step4) {
+                float e0 = t0, e1 = t1, e2 = t2, e3 = t3;
+                for (int g = 1; g < nG; ++g) {
+                    const float tg = tab[g][(x0 >> (7 * g)) & 127];  // the same for x0 .. x0 + 3
+                    e0 += tg;
+                    e1 += tg;
+                    e2 += tg;
+                    e3 += tg;
+                }
+                visit(x0, e0);
+                visit(x0 + 1, e1);
+                visit(x0 + 2, e2);
+                visit(x0 + 3, e3);
+            }
+        } else {
+            for (uint64_t x0 = x0b + tid; x0 < x0e; x0 += blockDim.x) visit(x0, energy(x0));
         }
         if (PASS == 0) {
             for (int o = 16; o > 0; o >>= 1) lmin = fminf(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
