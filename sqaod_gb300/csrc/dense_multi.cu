@@ -47,6 +47,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "sq_common.cuh"
 #include "sq_kernels.h"
@@ -842,7 +843,10 @@ static size_t multi_smem_bytes(int N) {
 }
 
 static int multi_capacity(int N) {
+    // the last answer is cached; callers on several host threads share it
+    static std::mutex mu;
     static int cachedN = -1, cachedCap = 0;
+    std::lock_guard<std::mutex> lock(mu);
     if (N == cachedN) return cachedCap;
     int dev = 0, sms = 0, perSm = 0, optin = 0;
     cudaGetDevice(&dev);
