@@ -240,6 +240,11 @@ SQ103_API int sq103_bipartite_bf_range(const float *b0, const float *b1, const f
                                        float *Emin32, void *stream);
 SQ103_API int sq103_bipartite_bf_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
                                         const uint64_t *pairs, int n, double *E, void *stream);
+/* The refines with FP64 couplings (the double-precision searchers screen with
+ * the fp32-rounded couplings and re-evaluate the candidates here). */
+SQ103_API int sq103_dense_bf_refine64(const double *W, int N, const uint64_t *x, int n, double *E, void *stream);
+SQ103_API int sq103_bipartite_bf_refine64(const double *b0, const double *b1, const double *W, int N0, int N1,
+                                          const uint64_t *pairs, int n, double *E, void *stream);
 
 /* ------------------------------------------- handle layer: annealers */
 /* Mirrors annealer.inc:885-908.  Preferences are passed as strings, as the
@@ -333,6 +338,15 @@ SQ103_API int sq103_bg_annealer_get_trace(void *handle, uint32_t *bits, int nwor
  * tile_size_0 / tile_size_1 (bipartite). */
 
 SQ103_API int sq103_dg_bf_new(void **handle);
+/* The <double> searcher (the reference's CUDADenseGraphBFSearcher<double>): the
+ * other sq103_dg_bf_* functions take either handle.  It screens with the
+ * fp32-rounded couplings (the screening slack widened by twice their total
+ * rounding) and re-evaluates the candidates with the FP64 couplings, so Emin
+ * and the argmin set are those of the FP64 problem.  sq103_dg_bf_set_qubo64
+ * sets FP64 couplings on either handle; on a <double> handle sq103_dg_bf_set_qubo
+ * takes fp32 couplings as exact doubles. */
+SQ103_API int sq103_dg_bf64_new(void **handle);
+SQ103_API int sq103_dg_bf_set_qubo64(void *handle, const double *W, int N, int optimize);
 SQ103_API int sq103_dg_bf_delete(void *handle);
 SQ103_API int sq103_dg_bf_set_qubo(void *handle, const float *W, int N, int optimize);
 SQ103_API int sq103_dg_bf_get_problem_size(void *handle, int *N);
@@ -354,6 +368,10 @@ SQ103_API int sq103_dg_bf_search_subrange(void *handle, unsigned long long xBegi
 SQ103_API int sq103_dg_bf_get_E64(void *handle, double *E);
 
 SQ103_API int sq103_bg_bf_new(void **handle);
+/* The <double> bipartite searcher, as sq103_dg_bf64_new above (W: N1 x N0). */
+SQ103_API int sq103_bg_bf64_new(void **handle);
+SQ103_API int sq103_bg_bf_set_qubo64(void *handle, const double *b0, const double *b1, const double *W, int N0,
+                                     int N1, int optimize);
 SQ103_API int sq103_bg_bf_delete(void *handle);
 SQ103_API int sq103_bg_bf_set_qubo(void *handle, const float *b0, const float *b1, const float *W, int N0,
                                    int N1, int optimize);
@@ -368,6 +386,8 @@ SQ103_API int sq103_bg_bf_make_solution(void *handle);
 SQ103_API int sq103_bg_bf_search_range(void *handle, unsigned long long *curX0, unsigned long long *curX1,
                                        int *done);
 SQ103_API int sq103_bg_bf_search(void *handle);
+/* exact FP64 minimum found so far (negated for maximize) */
+SQ103_API int sq103_bg_bf_get_E64(void *handle, double *E);
 
 /* ------------------------------------- handle layer: batched annealer */
 /* Many independent dense instances annealed in lock-step: one persistent

@@ -1,8 +1,8 @@
 // api.h -- CUDA solver interfaces of the sqaod C++ solver API
 // (sqaodc/cuda/api.h:16-83 of the reference): Device, DeviceAssigner and the
 // CUDA flavours of the four solvers and the two formula sets.  Implemented for sm_103a by
-// libsqaod_gb300.so: the solvers for <float>, the formula sets for <float>
-// and <double>.
+// libsqaod_gb300.so: the annealers for <float>; the BF searchers and the
+// formula sets for <float> and <double>.
 #pragma once
 
 #include <sqaodc/common/Common.h>

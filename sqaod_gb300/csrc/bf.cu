@@ -292,8 +292,10 @@ __global__ void __launch_bounds__(kBfThreads) bf_bip_pass(const float *b0, const
     }
 }
 
-// FP64 energies of packed dense states, one warp per state
-__global__ void bf_dense_refine(const float *W, int N, const uint64_t *xs, int n, double *E) {
+// FP64 energies of packed dense states, one warp per state (W float, or double
+// for the double-precision searchers)
+template <class T>
+__global__ void bf_dense_refine(const T *W, int N, const uint64_t *xs, int n, double *E) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= n) return;
     uint64_t x = xs[w];
@@ -307,8 +309,9 @@ __global__ void bf_dense_refine(const float *W, int N, const uint64_t *xs, int n
     if (lane == 0) E[w] = s;
 }
 
-__global__ void bf_bip_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
-                              const uint64_t *pairs, int n, double *E) {
+template <class T>
+__global__ void bf_bip_refine(const T *b0, const T *b1, const T *W, int N0, int N1, const uint64_t *pairs, int n,
+                              double *E) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= n) return;
     uint64_t x0 = pairs[2 * w], x1 = pairs[2 * w + 1];
@@ -368,7 +371,13 @@ SQ103_API int sq103_dense_bf_range(const float *W, int N, uint64_t xBegin, uint6
 
 SQ103_API int sq103_dense_bf_refine(const float *W, int N, const uint64_t *x, int n, double *E, void *stream) {
     if (n <= 0) return 0;
-    bf_dense_refine<<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(W, N, x, n, E);
+    bf_dense_refine<float><<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(W, N, x, n, E);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_bf_refine64(const double *W, int N, const uint64_t *x, int n, double *E, void *stream) {
+    if (n <= 0) return 0;
+    bf_dense_refine<double><<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(W, N, x, n, E);
     return (int)cudaGetLastError();
 }
 
@@ -396,7 +405,14 @@ SQ103_API int sq103_bipartite_bf_range(const float *b0, const float *b1, const f
 SQ103_API int sq103_bipartite_bf_refine(const float *b0, const float *b1, const float *W, int N0, int N1,
                                         const uint64_t *pairs, int n, double *E, void *stream) {
     if (n <= 0) return 0;
-    bf_bip_refine<<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(b0, b1, W, N0, N1, pairs, n, E);
+    bf_bip_refine<float><<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(b0, b1, W, N0, N1, pairs, n, E);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_bipartite_bf_refine64(const double *b0, const double *b1, const double *W, int N0, int N1,
+                                          const uint64_t *pairs, int n, double *E, void *stream) {
+    if (n <= 0) return 0;
+    bf_bip_refine<double><<<(n * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(b0, b1, W, N0, N1, pairs, n, E);
     return (int)cudaGetLastError();
 }
 

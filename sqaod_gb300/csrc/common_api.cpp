@@ -234,5 +234,8 @@ template struct Solver<float>;
 template struct Annealer<float>;
 template struct DenseGraphBFSearcher<float>;
 template struct BipartiteGraphBFSearcher<float>;
+template struct Solver<double>;
+template struct DenseGraphBFSearcher<double>;
+template struct BipartiteGraphBFSearcher<double>;
 
 }  // namespace sqaod

@@ -56,6 +56,14 @@ __global__ void sym_check_kernel(const float *W, int N, int ld, int *bad) {
     if (__syncthreads_or(mismatch) && tx == 0 && ty == 0) atomicOr(bad, 1);
 }
 
+// a matrix with row stride = columns
+template <class real>
+static std::vector<real> dense_copy(const sq::MatrixType<real> &M) {
+    std::vector<real> d((size_t)M.rows * M.cols);
+    for (int i = 0; i < M.rows; ++i)
+        memcpy(d.data() + (size_t)i * M.cols, M.data + (size_t)i * M.stride, sizeof(real) * M.cols);
+    return d;
+}
 // host check of int8 bits (0 / 1) or spins (-1 / +1)
 static void check_values(const int8_t *v, size_t n, bool spins, const char *fn) {
     for (size_t i = 0; i < n; ++i) {
@@ -925,6 +933,32 @@ public:
         float sgn = om == sq::optMaximize ? -1.f : 1.f;
         for (int r = 0; r < N_; ++r)
             for (int c = 0; c < N_; ++c) W_[(size_t)r * N_ + c] = sgn * W(r, c);
+        W64_.clear();
+        extraSlack_ = 0.;
+        setState(solProblemSet);
+    }
+
+    // The FP64 problem of the <double> searcher: the screening runs on the
+    // fp32-rounded couplings, its slack widened by twice their total rounding
+    // (a bound on how far any state's fp32 energy moves), and the candidates are
+    // re-evaluated with the FP64 couplings.
+    void setQUBO64(const double *W, int N, sq::OptimizeMethod om) {
+        throwErrorIf(N <= 0, "%s, Shape does not match.", __func__);
+        throwErrorIf(!sq::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
+        throwErrorIf(63 < N, "N must be smaller than 64, N=%d.", N);
+        clearState(solProblemSet);
+        N_ = N;
+        om_ = om;
+        const double sgn = om == sq::optMaximize ? -1. : 1.;
+        W64_.resize((size_t)N * N);
+        W_.resize((size_t)N * N);
+        double r = 0.;
+        for (size_t i = 0; i < W64_.size(); ++i) {
+            W64_[i] = sgn * W[i];
+            W_[i] = (float)W64_[i];
+            r += std::fabs(W64_[i] - (double)W_[i]);
+        }
+        extraSlack_ = 2. * r;
         setState(solProblemSet);
     }
 
@@ -937,6 +971,12 @@ public:
         SQ_CHECK(cudaMemcpyAsync(d_W_.p, W_.data(), sizeof(float) * N_ * N_, cudaMemcpyHostToDevice, st_.get()));
         d_ws_.ensure(sq103_bf_workspace_bytes(N_));
         slack_ = bf_slack(W_);
+        if (!W64_.empty()) {
+            d_W64_.ensure((size_t)N_ * N_);
+            SQ_CHECK(cudaMemcpyAsync(d_W64_.p, W64_.data(), sizeof(double) * N_ * N_, cudaMemcpyHostToDevice,
+                                     st_.get()));
+            slack_ = (float)((double)slack_ + extraSlack_ * (1. + 1e-6));  // rounded up past the cast
+        }
         res_.reset();
         xList_.clear();
         st_.sync();
@@ -1027,7 +1067,10 @@ private:
         std::vector<double> E(count);
         if (count > 0) {
             d_E_.ensure(count);
-            SQ_CHECK(sq103_dense_bf_refine(d_W_.p, N_, d_cand_.p, count, d_E_.p, st_.get()));
+            if (W64_.empty())
+                SQ_CHECK(sq103_dense_bf_refine(d_W_.p, N_, d_cand_.p, count, d_E_.p, st_.get()));
+            else
+                SQ_CHECK(sq103_dense_bf_refine64(d_W64_.p, N_, d_cand_.p, count, d_E_.p, st_.get()));
             SQ_CHECK(cudaMemcpyAsync(cand.data(), d_cand_.p, sizeof(uint64_t) * count, cudaMemcpyDeviceToHost, st_.get()));
             SQ_CHECK(cudaMemcpyAsync(E.data(), d_E_.p, sizeof(double) * count, cudaMemcpyDeviceToHost, st_.get()));
             st_.sync();
@@ -1037,12 +1080,15 @@ private:
 
     Stream st_;
     std::vector<float> W_;
+    std::vector<double> W64_;  // the FP64 couplings of a <double> problem (empty otherwise)
     DevBuf<float> d_W_;
+    DevBuf<double> d_W64_;
     DevBuf<unsigned char> d_ws_;
     DevBuf<uint64_t> d_cand_;
     DevBuf<double> d_E_;
     BfResult<uint64_t> res_;
     float slack_ = 0.f;
+    double extraSlack_ = 0.;
     sq::BitSetArray xList_;
     Vector E_;
 };
@@ -1083,8 +1129,42 @@ public:
         for (int i = 0; i < N1_; ++i) b1_[i] = sgn * b1(i);
         for (int i = 0; i < N1_; ++i)
             for (int j = 0; j < N0_; ++j) W_[(size_t)i * N0_ + j] = sgn * W(i, j);
+        b064_.clear();
+        b164_.clear();
+        W64_.clear();
+        extraSlack_ = 0.;
         setState(solProblemSet);
     }
+
+    // The FP64 problem of the <double> searcher (W: N1 x N0): fp32-rounded
+    // screening with the slack widened by twice the total rounding, FP64
+    // re-evaluation of the candidates.
+    void setQUBO64(const double *b0, const double *b1, const double *W, int N0, int N1, sq::OptimizeMethod om) {
+        throwErrorIf(N0 <= 0 || N1 <= 0, "%s, Shape does not match.", __func__);
+        throwErrorIf(63 < N0, "N0 must be smaller than 64, N0=%d.", N0);
+        throwErrorIf(63 < N1, "N1 must be smaller than 64, N1=%d.", N1);
+        clearState(solProblemSet);
+        N0_ = N0;
+        N1_ = N1;
+        om_ = om;
+        const double sgn = om == sq::optMaximize ? -1. : 1.;
+        double r = 0.;
+        auto round = [&](const double *src, size_t n, std::vector<double> &v64, std::vector<float> &v32) {
+            v64.resize(n);
+            v32.resize(n);
+            for (size_t i = 0; i < n; ++i) {
+                v64[i] = sgn * src[i];
+                v32[i] = (float)v64[i];
+                r += std::fabs(v64[i] - (double)v32[i]);
+            }
+        };
+        round(b0, N0, b064_, b0_);
+        round(b1, N1, b164_, b1_);
+        round(W, (size_t)N0 * N1, W64_, W_);
+        extraSlack_ = 2. * r;
+        setState(solProblemSet);
+    }
+    double EminExact() const { return om_ == sq::optMaximize ? -res_.Emin : res_.Emin; }
 
     void prepare() override {
         throwErrorIfProblemNotSet();
@@ -1104,6 +1184,16 @@ public:
         all.insert(all.end(), b0_.begin(), b0_.end());
         all.insert(all.end(), b1_.begin(), b1_.end());
         slack_ = bf_slack(all);
+        if (!W64_.empty()) {
+            d_b064_.ensure(N0_);
+            d_b164_.ensure(N1_);
+            d_W64_.ensure((size_t)N0_ * N1_);
+            SQ_CHECK(cudaMemcpyAsync(d_b064_.p, b064_.data(), sizeof(double) * N0_, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(d_b164_.p, b164_.data(), sizeof(double) * N1_, cudaMemcpyHostToDevice, st_.get()));
+            SQ_CHECK(cudaMemcpyAsync(d_W64_.p, W64_.data(), sizeof(double) * N0_ * N1_, cudaMemcpyHostToDevice,
+                                     st_.get()));
+            slack_ = (float)((double)slack_ + extraSlack_ * (1. + 1e-6));  // rounded up past the cast
+        }
         res_.reset();
         xList_.clear();
         st_.sync();
@@ -1195,7 +1285,12 @@ private:
         std::vector<double> E(count);
         if (count > 0) {
             d_E_.ensure(count);
-            SQ_CHECK(sq103_bipartite_bf_refine(d_b0_.p, d_b1_.p, d_W_.p, N0_, N1_, d_cand_.p, count, d_E_.p, st_.get()));
+            if (W64_.empty())
+                SQ_CHECK(sq103_bipartite_bf_refine(d_b0_.p, d_b1_.p, d_W_.p, N0_, N1_, d_cand_.p, count, d_E_.p,
+                                                   st_.get()));
+            else
+                SQ_CHECK(sq103_bipartite_bf_refine64(d_b064_.p, d_b164_.p, d_W64_.p, N0_, N1_, d_cand_.p, count,
+                                                     d_E_.p, st_.get()));
             SQ_CHECK(cudaMemcpyAsync(raw.data(), d_cand_.p, sizeof(uint64_t) * 2 * count, cudaMemcpyDeviceToHost, st_.get()));
             SQ_CHECK(cudaMemcpyAsync(E.data(), d_E_.p, sizeof(double) * count, cudaMemcpyDeviceToHost, st_.get()));
             st_.sync();
@@ -1208,7 +1303,10 @@ private:
 
     Stream st_;
     std::vector<float> b0_, b1_, W_;
+    std::vector<double> b064_, b164_, W64_;  // the FP64 problem of a <double> searcher (empty otherwise)
     DevBuf<float> d_b0_, d_b1_, d_W_;
+    DevBuf<double> d_b064_, d_b164_, d_W64_;
+    double extraSlack_ = 0.;
     DevBuf<unsigned char> d_ws_;
     DevBuf<uint64_t> d_cand_;
     DevBuf<double> d_E_;
@@ -1216,6 +1314,107 @@ private:
     float slack_ = 0.f;
     sq::BitSetPairArray xList_;
     Vector E_;
+};
+
+// ---------------------------------------------- double-precision BF searchers
+// The reference's <double> searchers (CUDADenseGraphBFSearcher<double>, ...):
+// a float searcher carries the FP64 problem (setQUBO64) and does the work, so
+// Emin and the argmin set are those of the FP64 couplings.  Preferences live
+// in both objects; energies are returned as the FP64 minimum.
+class DenseBFSearcher64 : public sq::cuda::DenseGraphBFSearcher<double> {
+public:
+    typedef sq::MatrixType<double> Matrix;
+    typedef sq::VectorType<double> Vector;
+
+    DenseBFSearcher64() { tileSize_ = 1 << 18; }
+    DenseBFSearcher &inner() { return f_; }
+
+    void assignDevice(sq::cuda::Device &device) override { f_.assignDevice(device); }
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::DenseGraphBFSearcher<double>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+    void setPreference(const sq::Preference &pref) override {
+        f_.setPreference(pref);
+        sq::DenseGraphBFSearcher<double>::setPreference(pref);
+    }
+    void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
+        std::vector<double> d = dense_copy(W);
+        setQUBO64(d.data(), W.rows, om);
+    }
+    void setQUBO64(const double *W, int N, sq::OptimizeMethod om) {
+        f_.setQUBO64(W, N, om);
+        N_ = N;
+    }
+    void prepare() override { f_.prepare(); }
+    bool searchRange(sq::PackedBitSet *curXEnd) override { return f_.searchRange(curXEnd); }
+    void search() override { f_.search(); }
+    void calculate_E() override { f_.calculate_E(); }
+    void makeSolution() override { f_.makeSolution(); }
+    const sq::BitSetArray &get_x() const override { return f_.get_x(); }
+    const Vector &get_E() const override {
+        const int n = f_.get_E().size;
+        E_.resize(n);
+        for (int i = 0; i < n; ++i) E_(i) = f_.EminExact();
+        return E_;
+    }
+
+private:
+    mutable DenseBFSearcher f_;
+    mutable Vector E_;
+};
+
+class BipartiteBFSearcher64 : public sq::cuda::BipartiteGraphBFSearcher<double> {
+public:
+    typedef sq::MatrixType<double> Matrix;
+    typedef sq::VectorType<double> Vector;
+
+    BipartiteBFSearcher64() {
+        tileSize0_ = 8192;
+        tileSize1_ = 8192;
+    }
+    BipartiteBFSearcher &inner() { return f_; }
+
+    void assignDevice(sq::cuda::Device &device) override { f_.assignDevice(device); }
+    sq::Preferences getPreferences() const override {
+        sq::Preferences prefs = sq::BipartiteGraphBFSearcher<double>::getPreferences();
+        prefs.pushBack(sq::Preference(sq::pnDevice, "cuda"));
+        return prefs;
+    }
+    void setPreference(const sq::Preference &pref) override {
+        f_.setPreference(pref);
+        sq::BipartiteGraphBFSearcher<double>::setPreference(pref);
+    }
+    void setQUBO(const Vector &b0, const Vector &b1, const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.cols != b0.size || W.rows != b1.size, "%s, Shape does not match.", __func__);
+        std::vector<double> d = dense_copy(W);
+        setQUBO64(b0.data, b1.data, d.data(), b0.size, b1.size, om);
+    }
+    void setQUBO64(const double *b0, const double *b1, const double *W, int N0, int N1, sq::OptimizeMethod om) {
+        f_.setQUBO64(b0, b1, W, N0, N1, om);
+        N0_ = N0;
+        N1_ = N1;
+    }
+    void prepare() override { f_.prepare(); }
+    bool searchRange(sq::PackedBitSet *curX0, sq::PackedBitSet *curX1) override {
+        return f_.searchRange(curX0, curX1);
+    }
+    void search() override { f_.search(); }
+    void calculate_E() override { f_.calculate_E(); }
+    void makeSolution() override { f_.makeSolution(); }
+    const sq::BitSetPairArray &get_x() const override { return f_.get_x(); }
+    const Vector &get_E() const override {
+        const int n = f_.get_E().size;
+        E_.resize(n);
+        for (int i = 0; i < n; ++i) E_(i) = f_.EminExact();
+        return E_;
+    }
+
+private:
+    mutable BipartiteBFSearcher f_;
+    mutable Vector E_;
 };
 
 // ===================================================== batched annealer
@@ -1612,14 +1811,6 @@ static std::vector<MatRow<real>> mat_rows(const sq::MatrixType<real> &m) {
     for (int r = 0; r < m.rows; ++r) rows.push_back(MatRow<real>{&m, r});
     return rows;
 }
-// a matrix with row stride = columns
-template <class real>
-static std::vector<real> dense_copy(const sq::MatrixType<real> &M) {
-    std::vector<real> d((size_t)M.rows * M.cols);
-    for (int i = 0; i < M.rows; ++i)
-        memcpy(d.data() + (size_t)i * M.cols, M.data + (size_t)i * M.stride, sizeof(real) * M.cols);
-    return d;
-}
 template <class real>
 static void to_vector(sq::VectorType<real> *E, const std::vector<double> &e) {
     E->resize((int)e.size());
@@ -2005,6 +2196,14 @@ DenseGraphBFSearcher<float> *newDenseGraphBFSearcher<float>() {
 template <>
 BipartiteGraphBFSearcher<float> *newBipartiteGraphBFSearcher<float>() {
     return new sq103::BipartiteBFSearcher();
+}
+template <>
+DenseGraphBFSearcher<double> *newDenseGraphBFSearcher<double>() {
+    return new sq103::DenseBFSearcher64();
+}
+template <>
+BipartiteGraphBFSearcher<double> *newBipartiteGraphBFSearcher<double>() {
+    return new sq103::BipartiteBFSearcher64();
 }
 template <>
 DenseGraphFormulas<float> *newDenseGraphFormulas<float>() {

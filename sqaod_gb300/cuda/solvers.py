@@ -6,7 +6,8 @@ dense_graph_bf_searcher,bipartite_graph_bf_searcher}.py over the base
 classes of sqaodpy/sqaod/common/*_base.py.  Every method forwards to one
 handle-layer entry point of the C ABI (include/sqaod_gb300.h).
 
-Only dtype=numpy.float32 is provided; other dtypes raise.
+The annealers take dtype numpy.float32; the brute-force searchers float32 or
+float64 (the <double> searchers, exact FP64 minima); other dtypes raise.
 """
 import ctypes
 
@@ -46,13 +47,21 @@ def _parse_prefs(s):
     return out
 
 
+def _check_bf_dtype(dtype):
+    """The brute-force searchers come in float32 and float64 (the <double> searchers)."""
+    d = np.dtype(np.float32 if dtype is None else dtype)
+    if d not in (np.float32, np.float64):
+        raise RuntimeError("dtype %s is not provided: the searchers compute in float32 or float64." % d)
+    return d.type
+
+
 class _Handle:
     _prefix = None
 
-    def __init__(self):
+    def __init__(self, new_name=None):
         self._L = lib()
         h = ctypes.c_void_p()
-        call(self._fn('new'), ctypes.byref(h))
+        call(getattr(self._L, new_name) if new_name else self._fn('new'), ctypes.byref(h))
         self._h = h
 
     def _fn(self, name):
@@ -406,8 +415,8 @@ class DenseGraphBFSearcher(_Handle):
     _prefix = 'sq103_dg_bf'
 
     def __init__(self, W, optimize, dtype, prefdict):
-        self.dtype = _check_dtype(dtype)
-        super().__init__()
+        self.dtype = _check_bf_dtype(dtype)
+        super().__init__('sq103_dg_bf64_new' if self.dtype is np.float64 else None)
         self._optimize = common.minimize
         if W is not None:
             self.set_qubo(W, optimize)
@@ -417,7 +426,8 @@ class DenseGraphBFSearcher(_Handle):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
         om = _c_int(common.optimize_flag(optimize))
-        common.submit_symmetric(W, self.dtype, lambda w: self._call('set_qubo', ptr(w), _c_int(w.shape[0]), om))
+        fn = 'set_qubo64' if self.dtype is np.float64 else 'set_qubo'
+        common.submit_symmetric(W, self.dtype, lambda w: self._call(fn, ptr(w), _c_int(w.shape[0]), om))
         self._optimize = optimize
 
     def get_problem_size(self):
@@ -433,6 +443,8 @@ class DenseGraphBFSearcher(_Handle):
         E = np.zeros(cap, np.float32)
         n = _c_int()
         self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        if self.dtype is np.float64:  # every solution has the exact FP64 minimum
+            return np.full(n.value, self.get_E64(), np.float64)
         return E[:n.value].copy()
 
     def get_x(self):
@@ -478,8 +490,8 @@ class BipartiteGraphBFSearcher(_Handle):
     _prefix = 'sq103_bg_bf'
 
     def __init__(self, b0, b1, W, optimize, dtype, prefdict):
-        self.dtype = _check_dtype(dtype)
-        super().__init__()
+        self.dtype = _check_bf_dtype(dtype)
+        super().__init__('sq103_bg_bf64_new' if self.dtype is np.float64 else None)
         self._optimize = common.minimize
         if W is not None:
             self.set_qubo(b0, b1, W, optimize)
@@ -489,8 +501,8 @@ class BipartiteGraphBFSearcher(_Handle):
         b0, b1, W = common.fix_type([np.asarray(b0), np.asarray(b1), np.asarray(W)], self.dtype)
         if W.ndim != 2 or W.shape != (len(b1), len(b0)):
             raise RuntimeError('dimension mismatch for b0, b1, W.')
-        self._call('set_qubo', ptr(b0), ptr(b1), ptr(W), _c_int(len(b0)), _c_int(len(b1)),
-                   _c_int(common.optimize_flag(optimize)))
+        self._call('set_qubo64' if self.dtype is np.float64 else 'set_qubo', ptr(b0), ptr(b1), ptr(W),
+                   _c_int(len(b0)), _c_int(len(b1)), _c_int(common.optimize_flag(optimize)))
         self._optimize = optimize
 
     def get_problem_size(self):
@@ -507,6 +519,8 @@ class BipartiteGraphBFSearcher(_Handle):
         E = np.zeros(cap, np.float32)
         n = _c_int()
         self._call('get_E', ptr(E), _c_int(cap), ctypes.byref(n))
+        if self.dtype is np.float64:  # every solution has the exact FP64 minimum
+            return np.full(n.value, self.get_E64(), np.float64)
         return E[:n.value].copy()
 
     def get_x(self):
@@ -534,6 +548,12 @@ class BipartiteGraphBFSearcher(_Handle):
 
     def search(self):
         self._call('search')
+
+    def get_E64(self):
+        """Exact FP64 minimum found so far (negated for maximize)."""
+        e = ctypes.c_double()
+        self._call('get_E64', ctypes.byref(e))
+        return e.value
 
 
 def dense_graph_annealer(W=None, optimize=common.minimize, dtype=np.float32, **prefs):

@@ -41,6 +41,7 @@ def test_cpp_api_symbols_exported(lib):
     for sym in ("sqaod::cuda::newDenseGraphAnnealer<float>", "sqaod::cuda::newBipartiteGraphAnnealer<float>",
                 "sqaod::cuda::newDenseGraphBFSearcher<float>", "sqaod::cuda::newBipartiteGraphBFSearcher<float>",
                 "sqaod::cuda::newDenseGraphFormulas<float>", "sqaod::cuda::newBipartiteGraphFormulas<float>",
+                "sqaod::cuda::newDenseGraphBFSearcher<double>", "sqaod::cuda::newBipartiteGraphBFSearcher<double>",
                 "sqaod::deleteInstance", "sqaod::cuda::newDevice"):
         assert sym in out, sym
 
@@ -168,6 +169,12 @@ void use() {
     sq::deleteInstance(f);
     sq::cuda::BipartiteGraphFormulas<float> *g = sq::cuda::newBipartiteGraphFormulas<float>();
     sq::deleteInstance(g);
+    sq::cuda::DenseGraphBFSearcher<double> *s = sq::cuda::newDenseGraphBFSearcher<double>();
+    s->setQUBO(Wd, sq::optMinimize);
+    s->search();
+    const sq::VectorType<double> &Es = s->get_E();
+    (void)Es;
+    sq::deleteInstance(s);
 }
 ''')
     import os
