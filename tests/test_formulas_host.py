@@ -38,3 +38,14 @@ def test_shape_and_type_checks():
     with pytest.raises(RuntimeError, match="dimension mismatch"):
         f.bipartite_graph_batch_calculate_E_2d(b0, b1, Wb, np.zeros((4, 2), np.int8), np.zeros((4, 2), np.int8),
                                                F32)
+
+
+def test_searcher_dtypes():
+    # the BF searchers come in float32 and float64; other dtypes raise before any device work
+    for make in (lambda d: sq.cuda.dense_graph_bf_searcher(dtype=d),
+                 lambda d: sq.cuda.bipartite_graph_bf_searcher(dtype=d)):
+        with pytest.raises(RuntimeError, match="float32 or float64"):
+            make(np.float16)
+    # the annealers are float32 only
+    with pytest.raises(RuntimeError, match="float32 only"):
+        sq.cuda.dense_graph_annealer(dtype=np.float64)
