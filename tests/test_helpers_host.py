@@ -1,6 +1,7 @@
 """Python helpers above the solver API that need no GPU: make_summary and
 unique_x (sqaodpy/sqaod/common/summary.py)."""
 import numpy as np
+import pytest
 
 import sqaod_gb300 as sq
 
@@ -37,3 +38,23 @@ def test_unique_x_of_bipartite_pairs_orders_by_x1_first():
     pairs = [(bits("10"), bits("01")), (bits("01"), bits("10")), (bits("00"), bits("01")), (bits("10"), bits("01"))]
     u = sq.unique_x(pairs)
     assert [(a.tolist(), b.tolist()) for a, b in u] == [([0, 0], [0, 1]), ([1, 0], [0, 1]), ([0, 1], [1, 0])]
+
+
+def test_batch_routing_threshold_rules():
+    # host-side rules of the batch's routing threshold (no device work before prepare)
+    from sqaod_gb300.batch import DenseBatchAnnealer
+    b = DenseBatchAnnealer()
+    with pytest.raises(sq.SqaodError, match="must not be negative"):
+        b.set_multicta_min_n(-1)
+    b.set_multicta_min_n(0)
+    assert b.multicta_count() == 0
+
+
+def test_checkpoint_needs_a_prepared_annealer():
+    a = sq.cuda.dense_graph_annealer()
+    state = {"q": np.ones((2, 4), np.int8), "F": np.zeros((2, 4), np.float32), "seed": 1, "step": 0,
+             "since_refresh": 0}
+    with pytest.raises(sq.SqaodError, match="not set"):
+        a.set_checkpoint(state)
+    with pytest.raises(RuntimeError, match="same shape"):
+        a.set_checkpoint(dict(state, F=np.zeros((3, 4), np.float32)))
