@@ -207,7 +207,7 @@ class DenseTask(ctypes.Structure):
                 ("status", ctypes.c_void_p), ("seed", ctypes.c_uint64), ("step0", ctypes.c_uint32),
                 ("N", ctypes.c_int), ("m", ctypes.c_int), ("ldJ", ctypes.c_int), ("algo", ctypes.c_int),
                 ("nSteps", ctypes.c_int), ("ws", ctypes.c_void_p), ("wsBytes", ctypes.c_ulonglong),
-                ("flags", ctypes.c_int)]
+                ("flags", ctypes.c_int), ("J64", ctypes.c_void_p), ("h64", ctypes.c_void_p)]
 
 
 def cpu_reference(W, steps, seed=0, min_seconds=0.0, warmup=1):
@@ -234,6 +234,25 @@ def cpu_reference(W, steps, seed=0, min_seconds=0.0, warmup=1):
             break
     dt = time.perf_counter() - t0
     return N * N_TROTTERS * n / dt, a.workers, dt, n
+
+
+CPU_LEG_STEPS, CPU_LEG_MIN_SECONDS = 20, 10.0
+
+
+def cpu_leg(steps, warmup, min_seconds=CPU_LEG_MIN_SECONDS):
+    """The reference CPU annealer timed in a fresh process (python bench.py
+    --cpu-leg): no torch, no GPU threads beside the OpenMP workers, one thread
+    per host core.  The headline line's cpu_baseline and --impl reference both
+    use it, with the same sampled schedule positions and minimum duration, so
+    the two figures measure the same thing.  Returns (trials/s, cores,
+    seconds, steps run)."""
+    env = dict(os.environ)
+    env["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+    out = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", "--steps", str(steps),
+                          "--warmup", str(warmup), "--min-seconds", str(min_seconds)],
+                         capture_output=True, text=True, env=env, check=True)
+    r = json.loads(out.stdout.strip().splitlines()[-1])
+    return r["value"], r["cores"], r["seconds"], r["steps"]
 
 
 def _sym_uniform(rng, N):
@@ -490,7 +509,10 @@ class BipartiteTask(ctypes.Structure):
                 ("trace", ctypes.c_void_p), ("accepted", ctypes.c_void_p), ("G", ctypes.c_void_p),
                 ("beta", ctypes.c_void_p), ("Gs", ctypes.c_float), ("betas", ctypes.c_float),
                 ("seed", ctypes.c_uint64), ("step0", ctypes.c_uint32), ("N0", ctypes.c_int), ("N1", ctypes.c_int),
-                ("m", ctypes.c_int), ("algo", ctypes.c_int), ("nSteps", ctypes.c_int)]
+                ("m", ctypes.c_int), ("algo", ctypes.c_int), ("nSteps", ctypes.c_int),
+                ("J64", ctypes.c_void_p), ("h0_64", ctypes.c_void_p), ("h1_64", ctypes.c_void_p),
+                ("digits1", ctypes.c_void_p), ("digits0", ctypes.c_void_p), ("spinsBf16", ctypes.c_void_p),
+                ("status", ctypes.c_void_p)]
 
 
 def _timed_steps(stream, flush, K, fn):
@@ -719,7 +741,7 @@ def run_reference(args, rank):
     from oracle import build as ob
     ob.build_oracle()
     ref_kind = "port"
-    val, cores, dt, n = cpu_reference(W, args.steps, warmup=args.warmup)
+    val, cores, dt, n = cpu_leg(CPU_LEG_STEPS, args.warmup)
     line = {"impl": "reference", "metric": "spin-flip trials/s (dense SQA coloring, N=4096 m=256)",
             "value": val, "unit": "trials/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * dt / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
@@ -727,7 +749,9 @@ def run_reference(args, rank):
             "config": {"workload": "dense SQA coloring N=4096 m=256 beta=50 G=5*0.99^k (619-step schedule)",
                        "N": N_SPINS, "m": N_TROTTERS, "algorithm": "coloring"},
             "cpu_baseline": {"value": val, "unit": "trials/s", "cores": cores, "kind": ref_kind,
-                             "sample": "%d annealOneSteps of the 619-step schedule (sampled evenly), %.1f s" % (n, dt)},
+                             "sample": "%d annealOneSteps (1,048,576 trials each) at %d positions sampled evenly "
+                                       "over the 619-step schedule, after %d warm-up steps, %.1f s, in a fresh "
+                                       "process" % (n, CPU_LEG_STEPS, args.warmup, dt)},
             "e2e": {"value": val, "unit": "trials/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -757,7 +781,15 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16, help="batched mode: instances solved on the plain path")
     ap.add_argument("--multicta-min-n", type=int, default=None,
                     help="batched mode: instances of at least this N take the one-CTA-per-trotter sweep (default 1024)")
+    ap.add_argument("--cpu-leg", action="store_true", help="internal: time the CPU reference annealer alone")
+    ap.add_argument("--min-seconds", type=float, default=CPU_LEG_MIN_SECONDS, help="--cpu-leg: minimum duration")
     args = ap.parse_args()
+
+    if args.cpu_leg:
+        val, cores, dt, n = cpu_reference(problem(N_SPINS), args.steps, min_seconds=args.min_seconds,
+                                          warmup=args.warmup)
+        print(json.dumps({"value": val, "cores": cores, "seconds": dt, "steps": n}), flush=True)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -804,7 +836,21 @@ def main():
     seed = 1000 + rank
     assert L.sq103_dense_hamiltonian(P(dW), N, N, 0, P(dh), P(dJ), N, P(c32), P(c64), P(scratch), sp) == 0
     assert L.sq103_randomize_spins(P(q), N, m, ctypes.c_uint64(seed), ctypes.c_uint32(0), 0, sp) == 0
-    assert L.sq103_dense_field_refresh(P(dJ), N, P(q), P(F), N, m, sp) == 0
+    # the refresh the solver runs: tensor-core digit contraction for N >= 1024, else SIMT
+    L.sq103_tc_digits_bytes.restype = ctypes.c_ulonglong
+    L.sq103_tc_spins_bytes.restype = ctypes.c_ulonglong
+    use_tc = bool(L.sq103_dense_refresh_uses_tc(N))
+    digits = torch.empty(int(L.sq103_tc_digits_bytes(N, N)) if use_tc else 1, dtype=torch.uint8, device=dev)
+    abf = torch.empty(int(L.sq103_tc_spins_bytes(m, N)) if use_tc else 1, dtype=torch.uint8, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    if use_tc:
+        assert L.sq103_tc_make_digits(P(dJ), N, N, N, 0, P(digits), sp) == 0
+    dig_p = P(digits) if use_tc else None
+
+    def refresh_fields():
+        return L.sq103_dense_refresh(P(dJ), N, dig_p, P(abf), P(q), P(F), N, m, P(status), sp)
+
+    assert refresh_fields() == 0
     sched = schedule()
     K, Wm = args.steps, args.warmup
     spl = args.steps_per_launch
@@ -818,7 +864,6 @@ def main():
     L.sq103_dense_ws_bytes.restype = ctypes.c_ulonglong
     ws_bytes = int(L.sq103_dense_ws_bytes(N, m, spl))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
-    status = torch.zeros(1, dtype=torch.int32, device=dev)
     multi = bool(L.sq103_dense_multicta_ok(N, m, 1))
     refresh = spl == 8
 
@@ -832,8 +877,8 @@ def main():
             raise RuntimeError("sq103_dense_anneal failed: %d" % rc)
 
     def do_refresh():
-        if refresh and L.sq103_dense_field_refresh(P(dJ), N, P(q), P(F), N, m, sp) != 0:
-            raise RuntimeError("sq103_dense_field_refresh failed")
+        if refresh and refresh_fields() != 0:
+            raise RuntimeError("sq103_dense_refresh failed")
 
     step = 1
     for i in range(Wm):
@@ -875,6 +920,16 @@ def main():
     alg_bytes = accepted * 4.0 * N + 10.0 * N * m * spl                          # per launch
     achieved_gbs = float(alg_bytes.sum()) / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    # the field refresh of each timed unit (launched after the sweep, timed by the same events):
+    # 2 N^2 m algorithmic flops; the tensor-core path issues four digit contractions of that size
+    refresh_info = None
+    if refresh:
+        r_ms = float(sum(a.elapsed_time(b) for a, b in zip(mids, ends))) / K
+        flops = 2.0 * N * N * m
+        refresh_info = {"kernel": "tc_digit_gemm (tcgen05, 4 bf16 digit planes, exact)" if use_tc
+                        else "field_gemm_kernel (fp32 SIMT)", "ms_per_launch": r_ms,
+                        "algorithmic_tflops": flops / (r_ms / 1e3) / 1e12,
+                        "mma_tflops": (4.0 if use_tc else 1.0) * flops / (r_ms / 1e3) / 1e12}
 
     # -------- end to end through the solver-handle C ABI with host buffers: one
     # whole anneal of the 619-step schedule, as a user runs it (set_qubo uploads W,
@@ -906,10 +961,11 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and (N, m) == (N_SPINS, N_TROTTERS):
-        val, cores, dt, n = cpu_reference(W, 20, min_seconds=10.0)
+        val, cores, dt, n = cpu_leg(CPU_LEG_STEPS, args.warmup)
         cpu = {"value": val, "unit": "trials/s", "cores": cores, "kind": "port",
-               "sample": "%d annealOneSteps (1,048,576 trials each) of the same instance, G sampled evenly "
-                         "over the 619-step schedule, %.1f s" % (n, dt)}
+               "sample": "%d annealOneSteps (1,048,576 trials each) at %d positions sampled evenly over the "
+                         "619-step schedule, after %d warm-up steps, %.1f s, in a fresh process"
+                         % (n, CPU_LEG_STEPS, args.warmup, dt)}
 
     if rank == 0:
         traffic = _profiled_traffic("dense_sweep_multi N=%d m=%d steps=%d" % (N, m, spl))
@@ -927,12 +983,13 @@ def main():
                            "l2": "flushed between timed units (512 MB write)",
                            "kernel": "one CTA per trotter (cooperative)" if multi else "one CTA per instance",
                            "parallelism": "replicas" if world > 1 else "single instance"},
-                "e2e": e2e, "gpu_launches": K * (2 if refresh else 1),
+                "e2e": e2e, "gpu_launches": K * (1 + ((2 if use_tc else 1) if refresh else 0)),
                 "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
                              "frac": achieved_gbs / peak, "traffic": traffic, "peak_source": peak_kind,
                              "algorithmic_bytes_per_launch": float(alg_bytes.mean()),
                              "steps_per_launch": spl, "sweep_ms_per_launch": sweep_ms / K,
-                             "accepted_per_step": float(accepted.mean()) / spl},
+                             "accepted_per_step": float(accepted.mean()) / spl,
+                             "refresh": refresh_info},
                 "cpu_baseline": cpu, "clocks": clk.summary(), "wall_s": wall}
         print(json.dumps(line), flush=True)
     if dist:

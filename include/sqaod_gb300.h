@@ -57,6 +57,10 @@ extern "C" {
 SQ103_API const char *sq103_last_error(void);
 /* library version (1.0.3 of the reference API: sqaodc/common/defines.h:80) */
 SQ103_API int sq103_version(void);
+/* makes CUDA device devNo current for the calling thread: the solvers created
+ * and called on that thread run there (sqaod::cuda::Device + assignDevice,
+ * sqaodc/cuda/api.h:16-37) */
+SQ103_API int sq103_device_set(int devNo);
 
 /* ------------------------------------------------ kernel layer: dense */
 
@@ -82,7 +86,13 @@ typedef struct sq103_dense_task {
     int nSteps;
     void *ws;             /* optional device workspace for the multi-CTA sweep */
     unsigned long long wsBytes; /* its size; sq103_dense_ws_bytes(N, m, nSteps) */
-    int flags;            /* 0 = choose the kernel, 1 = one CTA per instance, 2 = one CTA per trotter */
+    int flags;            /* bits 0-1: 0 = choose the kernel, 1 = one CTA per instance, 2 = one CTA per
+                             trotter.  Test hooks of the one-CTA-per-trotter sweep: 16 = every bounded
+                             wait gives up after 1 ms (not 4 s); 32 = trotter 0 never publishes its accept
+                             words, so its neighbours' waits run out and the kernel ends with status 1 */
+    const double *J64;    /* optional FP64 couplings of a <double> problem (N x N, row stride N; J is their
+                             fp32 rounding): trials the fp32 path flags are decided from these */
+    const double *h64;    /* optional FP64 h of a <double> problem */
 } sq103_dense_task;
 
 /* workspace the multi-CTA sweep needs for nSteps steps (one 64-bit accept word per trotter and
@@ -98,6 +108,38 @@ SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
 SQ103_API int sq103_dense_anneal_pack(const sq103_dense_task *tasks, int n, void *stream);
 /* CTAs of the one-CTA-per-trotter sweep that can be resident at once for rows of N spins */
 SQ103_API int sq103_dense_multicta_capacity(int N);
+
+/* ------------------------------------------- tensor-core field refresh
+ * F[y][r] = sum_k q[y][k] B[r][k] on tcgen05 (operands by TMA, accumulators in
+ * TMEM); replaces the J.q contractions DeviceDotJqVec4
+ * (sqaodc/cuda/DeviceBatchedDot.cuh:247-262) and the cuBLAS SGEMMs of
+ * CUDABipartiteGraphAnnealer.cu:393-401.  B is held as four signed 8-bit digit
+ * planes of its 31-bit fixed-point value (exact in bf16); with +-1 spins every
+ * partial sum is an integer below 2^24, so the contraction is exact and the
+ * result is within the quantisation of B (2^-29 of max |B| per element) of the
+ * exact field, rounded once to fp32.  K < 2^17. */
+/* bytes of the digit buffer of an R x K matrix B (256-byte aligned allocation) */
+SQ103_API unsigned long long sq103_tc_digits_bytes(int R, int K);
+/* bytes of the bf16 spin scratch of m rows of K spins (16-byte aligned) */
+SQ103_API unsigned long long sq103_tc_spins_bytes(int m, int K);
+/* digit planes of B = J (R x K, row stride ldJ; transpose = 0) or B = J^T (J is
+ * K x R, row stride ldJ; transpose = 1) */
+SQ103_API int sq103_tc_make_digits(const float *J, int ldJ, int R, int K, int transpose, void *digits, void *stream);
+/* F (m x R, row stride ldF) from the digits and q (m x K int8, row stride ldq);
+ * spinsBf16: sq103_tc_spins_bytes(m, K) of scratch.  status: optional device word
+ * set to 1 when a bounded wait gave up.  flags: 0; test hooks 1 = the first K
+ * block's copies are never issued, 2 = waits give up after 1 ms. */
+SQ103_API int sq103_tc_refresh(const void *digits, int R, int K, const int8_t *q, int ldq, int m, void *spinsBf16,
+                               float *F, int ldF, int flags, int *status, void *stream);
+/* 1 when the dense annealers refresh N-spin fields on the tensor cores (N >= 1024) */
+SQ103_API int sq103_dense_refresh_uses_tc(int N);
+/* 1 when the bipartite annealers compute the half-step fields on the tensor cores
+ * (N0 N1 >= 2^20); the task then carries the digits of J and J^T */
+SQ103_API int sq103_bipartite_refresh_uses_tc(int N0, int N1);
+/* the dense refresh of every path: sq103_tc_refresh from `digits` (of J, R = K = N)
+ * when given, else sq103_dense_field_refresh */
+SQ103_API int sq103_dense_refresh(const float *J, int ldJ, const void *digits, void *spinsBf16, const int8_t *q,
+                                  float *F, int N, int m, int *status, void *stream);
 
 /* QUBO -> Ising (h, J, c); replaces DeviceDenseGraphFormulas::calculateHamiltonian
  * (sqaodc/cuda/DeviceFormulas.cpp:24-31).  scratch: N doubles. */
@@ -174,6 +216,13 @@ typedef struct sq103_bipartite_task {
     uint64_t seed;
     uint32_t step0;
     int N0, N1, m, algo, nSteps;
+    const double *J64, *h0_64, *h1_64; /* optional FP64 problem of a <double> annealer (J64 N1 x N0; J, h0,
+                                          h1 are its fp32 rounding): trials the fp32 path flags are
+                                          decided from these */
+    const void *digits1, *digits0;     /* optional: the half-step fields on the tensor cores from the
+                                          digits of J (for F1) and of J^T (for F0), sq103_tc_make_digits */
+    void *spinsBf16;                   /* their spin scratch, sq103_tc_spins_bytes(m, max(N0, N1)) */
+    int *status;                       /* optional status word (a bounded wait of the refresh gave up) */
 } sq103_bipartite_task;
 
 /* (sqaodc/cuda/DeviceFormulas.cpp:107-117). scratch: N0 + N1 doubles */
@@ -254,6 +303,17 @@ SQ103_API int sq103_bipartite_bf_refine64(const double *b0, const double *b1, co
  * "algorithm=...;n_trotters=...;precision=float;device=cuda". */
 
 SQ103_API int sq103_dg_annealer_new(void **handle);
+/* <double> annealer (sqaod::cuda::DenseGraphAnnealer<double>,
+ * sqaodc/cuda/CUDADenseGraphAnnealer.cu:607-608): every entry point below takes
+ * its handle too.  The FP64 problem is set with sq103_dg_annealer_set_qubo64 /
+ * set_hamiltonian64; the sweeps run on its fp32 rounding, every trial the fp32
+ * test flags is decided from the FP64 couplings, energies are FP64 sums
+ * (sq103_dg_annealer_get_E64), and G and beta are taken in fp32. */
+SQ103_API int sq103_dg_annealer64_new(void **handle);
+SQ103_API int sq103_dg_annealer_set_qubo64(void *handle, const double *W, int N, int optimize);
+SQ103_API int sq103_dg_annealer_set_hamiltonian64(void *handle, const double *h, const double *J, double c, int N);
+SQ103_API int sq103_dg_annealer_get_hamiltonian64(void *handle, double *h, double *J, double *c);
+SQ103_API int sq103_dg_annealer_get_system_E64(void *handle, double G, double beta, double *E);
 SQ103_API int sq103_dg_annealer_delete(void *handle);
 SQ103_API int sq103_dg_annealer_seed(void *handle, unsigned long long seed);
 SQ103_API int sq103_dg_annealer_set_qubo(void *handle, const float *W, int N, int optimize);
@@ -297,6 +357,14 @@ SQ103_API int sq103_dg_annealer_set_kernel(void *handle, int flags);
 SQ103_API int sq103_dg_annealer_get_trace(void *handle, uint32_t *bits, int nwords);
 
 SQ103_API int sq103_bg_annealer_new(void **handle);
+/* <double> bipartite annealer (CUDABipartiteGraphAnnealer.cu:647-648), as above */
+SQ103_API int sq103_bg_annealer64_new(void **handle);
+SQ103_API int sq103_bg_annealer_set_qubo64(void *handle, const double *b0, const double *b1, const double *W,
+                                           int N0, int N1, int optimize);
+SQ103_API int sq103_bg_annealer_set_hamiltonian64(void *handle, const double *h0, const double *h1,
+                                                  const double *J, double c, int N0, int N1);
+SQ103_API int sq103_bg_annealer_get_hamiltonian64(void *handle, double *h0, double *h1, double *J, double *c);
+SQ103_API int sq103_bg_annealer_get_system_E64(void *handle, double G, double beta, double *E);
 SQ103_API int sq103_bg_annealer_delete(void *handle);
 SQ103_API int sq103_bg_annealer_seed(void *handle, unsigned long long seed);
 SQ103_API int sq103_bg_annealer_set_qubo(void *handle, const float *b0, const float *b1, const float *W,
@@ -509,6 +577,12 @@ SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *do
 /* at most n large instances admitted at a time (default 8; dense: one CTA per
  * trotter, packed up to 8 per launch; bipartite: per-instance kernels) */
 SQ103_API int sq103_server_set_large_limit(void *handle, int n);
+/* Fault injection from the host (tests; no counterpart in the reference): writes
+ * `value` into the status word of active dense request `id`, in stream order, as a
+ * sweep that gave up a bounded device wait does.  Every dense request has its own
+ * status word; sq103_server_result of that request then fails (the request is still
+ * released when asked), and no other request is affected. */
+SQ103_API int sq103_server_inject_status(void *handle, int id, int value);
 /* ids of the requests completed since the last call (at most cap, in completion order) */
 SQ103_API int sq103_server_completed(void *handle, int *ids, int cap, int *n);
 

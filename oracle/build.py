@@ -16,7 +16,10 @@ import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("SQAOD_REFERENCE_ROOT", "/root/reference")
+# the reference tree: $SQAOD_REFERENCE_ROOT, else a directory named "reference"
+# beside this repository's root; build_ref() skips the build when it is absent
+REF_ROOT = os.environ.get("SQAOD_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def _run(cmd):

@@ -1106,22 +1106,124 @@ void orc_dg_replay(const float *h, const float *J, int N, int m, int algo,
     }
 }
 
+/*
+ * Same decisions as orc_dg_replay over nSteps consecutive annealOneSteps (step
+ * counters step0 .. step0 + nSteps - 1, trace of step s at trace + s * words),
+ * but with FP64 local fields kept resident: F[y][i] = sum_j J_ij q_yj is
+ * computed once (threads over trotters) and every flip the device reports adds
+ * -2 s J[x][:] to its trotter's row.  Each addend is an fp32 value, exact in
+ * FP64, so the fields stay within a few FP64 ulps of the direct dot products;
+ * the cost per step is N m trials plus N per accepted flip, which makes the
+ * benchmark size (N = 4096, m = 256) replayable.  J must be symmetric with a
+ * zero diagonal (the Ising J of the dense formulas).
+ */
+void orc_dg_replay_steps(const double *h, const double *J, int N, int m, int algo, uint64_t seed,
+                         uint32_t step0, int nSteps, const float *G, const float *beta, int8_t *q,
+                         const uint32_t *trace, double tol, orc_replay_stats *st) {
+    replay_ctx ctx = {tol, st};
+    double *F = (double *)malloc(sizeof(double) * (size_t)m * N);
+    if (!F) return;
+#pragma omp parallel
+    {
+        double *qd = (double *)malloc(sizeof(double) * (size_t)N);
+#pragma omp for schedule(static)
+        for (int y = 0; y < m; ++y) {
+            const int8_t *qy = q + (size_t)y * N;
+            for (int j = 0; j < N; ++j) qd[j] = qy[j];
+            for (int i = 0; i < N; ++i) {
+                const double *Ji = J + (size_t)i * N;
+                double s = 0.;
+                for (int j = 0; j < N; ++j) s += Ji[j] * qd[j];
+                F[(size_t)y * N + i] = s;
+            }
+        }
+        free(qd);
+    }
+    const size_t words = ((size_t)N * m + 31) / 32;
+    for (int s = 0; s < nSteps; ++s) {
+        const uint32_t *tr = trace + words * (size_t)s;
+        const uint32_t step = step0 + (uint32_t)s;
+        const double Gd = G[s], bd = beta[s];
+        const double twoDivM = 2. / m;
+        const double coef = log(tanh(Gd * bd / m)) / bd;
+        const double invKT = 1. / Gd;
+#define ORC_FLIP(Y, X)                                                   \
+    do {                                                                 \
+        int8_t *qy_ = q + (size_t)(Y) * N;                               \
+        double d_ = -2. * qy_[(X)];                                      \
+        double *Fy_ = F + (size_t)(Y) * N;                               \
+        const double *Jx_ = J + (size_t)(X) * N;                         \
+        for (int i_ = 0; i_ < N; ++i_) Fy_[i_] += d_ * Jx_[i_];         \
+        qy_[(X)] = (int8_t)-qy_[(X)];                                    \
+    } while (0)
+        if (algo == ORC_ALGO_NAIVE) {
+            const long long nTrials = (long long)N * m;
+            for (long long t = 0; t < nTrials; ++t) {
+                uint32_t w[4];
+                philox_draw(seed, (uint32_t)t, 0u, step, ORC_TAG_DNAIVE, w);
+                int y = mulhi_index(w[0], m), x = mulhi_index(w[1], N);
+                float u = unit_float(w[2]);
+                double qyx = q[(size_t)y * N + x];
+                int yl = (y + m - 1) % m, yr = (y + 1) % m;
+                double dE = twoDivM * qyx * ((double)h[x] + 2. * F[(size_t)y * N + x]) -
+                            qyx * (q[(size_t)yl * N + x] + q[(size_t)yr * N + x]) * coef;
+                if (replay_decide(&ctx, dE, bd, u, trace_bit(tr, t))) ORC_FLIP(y, x);
+            }
+        } else if (algo == ORC_ALGO_COLORING) {
+            const int m2 = (m / 2) * 2;
+            for (int k = 0; k < N; ++k)
+                for (int phase = 0; phase < 3; ++phase) {
+                    int yb, ye, ys;
+                    if (phase == 0) { yb = 0; ye = m2; ys = 2; }
+                    else if (phase == 1) { if (!(m % 2)) continue; yb = m - 1; ye = m; ys = 1; }
+                    else { yb = 1; ye = m2; ys = 2; }
+                    /* trotters of one phase are never ring neighbours: flipping at once is the same
+                       as evaluating the phase first */
+                    for (int y = yb; y < ye; y += ys) {
+                        uint32_t w[4];
+                        philox_draw(seed, (uint32_t)k, (uint32_t)y, step, ORC_TAG_DSWEEP, w);
+                        int x = mulhi_index(w[0], N);
+                        float u = unit_float(w[1]);
+                        double qyx = q[(size_t)y * N + x];
+                        int yl = (y + m - 1) % m, yr = (y + 1) % m;
+                        double dE = twoDivM * qyx * ((double)h[x] + 2. * F[(size_t)y * N + x]) -
+                                    qyx * (q[(size_t)yl * N + x] + q[(size_t)yr * N + x]) * coef;
+                        if (replay_decide(&ctx, dE, bd, u, trace_bit(tr, (long long)k * m + y))) ORC_FLIP(y, x);
+                    }
+                }
+        } else {
+            for (int y = 0; y < m; ++y)
+                for (int k = 0; k < N; ++k) {
+                    uint32_t w[4];
+                    philox_draw(seed, (uint32_t)k, (uint32_t)y, step, ORC_TAG_DSA, w);
+                    int x = mulhi_index(w[0], N);
+                    float u = unit_float(w[1]);
+                    double qyx = q[(size_t)y * N + x];
+                    double dE = 2. * qyx * ((double)h[x] + 2. * F[(size_t)y * N + x]);
+                    if (replay_decide(&ctx, dE, invKT, u, trace_bit(tr, (long long)k * m + y))) ORC_FLIP(y, x);
+                }
+        }
+#undef ORC_FLIP
+    }
+    free(F);
+}
+
 /* field on spin x of `side` in trotter y from the other side (FP64) */
-static double bg_field64(const float *J, int N0, int N1, const int8_t *q0, const int8_t *q1,
+static double bg_field64(const double *J, int N0, int N1, const int8_t *q0, const int8_t *q1,
                          int side, int y, int x) {
     double s = 0.;
     if (side == 1) {
-        const float *Jx = J + (size_t)x * N0;
+        const double *Jx = J + (size_t)x * N0;
         const int8_t *qf = q0 + (size_t)y * N0;
-        for (int j = 0; j < N0; ++j) s += (double)Jx[j] * qf[j];
+        for (int j = 0; j < N0; ++j) s += Jx[j] * qf[j];
     } else {
         const int8_t *qf = q1 + (size_t)y * N1;
-        for (int i = 0; i < N1; ++i) s += (double)J[(size_t)i * N0 + x] * qf[i];
+        for (int i = 0; i < N1; ++i) s += J[(size_t)i * N0 + x] * qf[i];
     }
     return s;
 }
 
-void orc_bg_replay(const float *h0, const float *h1, const float *J, int N0, int N1, int m,
+void orc_bg_replay(const double *h0, const double *h1, const double *J, int N0, int N1, int m,
                    int algo, uint64_t seed, uint32_t step, float G, float beta,
                    int8_t *q0, int8_t *q1, const uint32_t *trace, double tol,
                    orc_replay_stats *st) {
@@ -1147,7 +1249,7 @@ void orc_bg_replay(const float *h0, const float *h1, const float *J, int N0, int
                 if (side) x -= N0;
                 int Ns = side ? N1 : N0;
                 int8_t *qA = side ? q1 : q0;
-                const float *h = side ? h1 : h0;
+                const double *h = side ? h1 : h0;
                 double qyx = qA[(size_t)y * Ns + x];
                 double F = bg_field64(J, N0, N1, q0, q1, side, y, x);
                 double dE;
@@ -1171,7 +1273,7 @@ void orc_bg_replay(const float *h0, const float *h1, const float *J, int N0, int
         int side = hs == 0 ? 1 : 0;
         int Ns = side ? N1 : N0;
         int8_t *qA = side ? q1 : q0;
-        const float *h = side ? h1 : h0;
+        const double *h = side ? h1 : h0;
         for (int y = 0; y < m; ++y)
             for (int i = 0; i < Ns; ++i)
                 F[(size_t)y * Ns + i] = bg_field64(J, N0, N1, q0, q1, side, y, i);
@@ -1205,4 +1307,108 @@ void orc_bg_replay(const float *h0, const float *h1, const float *J, int N0, int
         bitBase += (long long)m * Ns;
     }
     free(F);
+}
+
+/* ========================== exact integer BF in Gray-code order (checker) ==== */
+typedef struct {
+    int64_t best;
+    uint64_t *list;
+    long long n, cap;
+    int overflow;
+} gray_worker;
+
+int orc_dg_bf_search_exact_int(const float *W, int N, int om, int cap, int nWorkers,
+                               double *Emin, uint64_t *xout, long long *nMin) {
+    if (N < 1 || N > 40) return -2;
+    int32_t *Wz = (int32_t *)malloc(sizeof(int32_t) * (size_t)N * N);
+    int32_t *diag = (int32_t *)malloc(sizeof(int32_t) * (size_t)N);
+    double tot = 0.;
+    int bad = 0;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            double w = om == 1 ? -(double)W[(size_t)i * N + j] : (double)W[(size_t)i * N + j];
+            if (w != floor(w) || W[(size_t)i * N + j] != W[(size_t)j * N + i]) bad = 1;
+            tot += fabs(w);
+            Wz[(size_t)i * N + j] = i == j ? 0 : (int32_t)w;
+            if (i == j) diag[i] = (int32_t)w;
+        }
+    if (bad || tot >= 1073741824.) {
+        free(Wz);
+        free(diag);
+        return -3;
+    }
+    const int nw = omp_workers(nWorkers);
+    const uint64_t total = 1ull << N;
+    gray_worker *ws = (gray_worker *)calloc(nw, sizeof(gray_worker));
+#pragma omp parallel num_threads(nw)
+    {
+        const int t = omp_tid();
+        gray_worker *me = &ws[t];
+        me->cap = 1 << 16;
+        me->list = (uint64_t *)malloc(sizeof(uint64_t) * me->cap);
+        const uint64_t n0 = total / nw * t + ORC_MIN((uint64_t)t, total % nw);
+        const uint64_t n1 = n0 + total / nw + ((uint64_t)t < total % nw ? 1 : 0);
+        if (n0 < n1) {
+            int32_t g[64];  /* g_k = sum_{j != k} W_kj x_j; packed bit b is variable N-1-b */
+            uint64_t v = n0 ^ (n0 >> 1);
+            int64_t E = 0;
+            for (int k = 0; k < N; ++k) {
+                int32_t s = 0;
+                for (int j = 0; j < N; ++j) s += Wz[(size_t)k * N + j] * (int32_t)((v >> (N - 1 - j)) & 1);
+                g[k] = s;
+                if ((v >> (N - 1 - k)) & 1) E += diag[k] + s;
+            }
+            me->best = E;
+            me->list[me->n++] = v;
+            for (uint64_t n = n0 + 1; n < n1; ++n) {
+                const int b = __builtin_ctzll(n);
+                const int k = N - 1 - b;
+                const int xk = (int)((v >> b) & 1);
+                const int32_t d = diag[k] + 2 * g[k];
+                E += xk ? -(int64_t)d : (int64_t)d;
+                const int32_t sgn = xk ? -1 : 1;
+                const int32_t *Wk = Wz + (size_t)k * N;
+                for (int j = 0; j < N; ++j) g[j] += sgn * Wk[j];
+                v ^= 1ull << b;
+                if (E <= me->best) {
+                    if (E < me->best) {
+                        me->best = E;
+                        me->n = 0;
+                        me->overflow = 0;
+                    }
+                    if (me->n < me->cap) me->list[me->n++] = v;
+                    else me->overflow = 1;
+                }
+            }
+        } else {
+            me->best = INT64_MAX;
+        }
+    }
+    int64_t best = INT64_MAX;
+    for (int t = 0; t < nw; ++t) best = ORC_MIN(best, ws[t].best);
+    long long count = 0;
+    int overflow = 0;
+    for (int t = 0; t < nw; ++t)
+        if (ws[t].best == best) {
+            count += ws[t].n;
+            overflow |= ws[t].overflow;
+        }
+    uint64_t *all = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)ORC_MAX(count, 1));
+    long long k = 0;
+    for (int t = 0; t < nw; ++t)
+        if (ws[t].best == best) {
+            memcpy(all + k, ws[t].list, sizeof(uint64_t) * ws[t].n);
+            k += ws[t].n;
+        }
+    qsort(all, (size_t)count, sizeof(uint64_t), cmp_u64);
+    int nout = (int)ORC_MIN((long long)cap, count);
+    memcpy(xout, all, sizeof(uint64_t) * nout);
+    *Emin = om == 1 ? -(double)best : (double)best;
+    *nMin = count;
+    for (int t = 0; t < nw; ++t) free(ws[t].list);
+    free(ws);
+    free(all);
+    free(Wz);
+    free(diag);
+    return overflow ? -4 : nout;
 }

@@ -22,7 +22,7 @@
  *
  * Parity pins: MT19937 and the AVX2-order dot are checked against the
  * reference's own Random.cpp / Dot_SIMD.cpp compiled from source (oracle/_ref,
- * built by oracle/build_ref.sh); formulas and BF results are checked against
+ * built by oracle/build.py); formulas and BF results are checked against
  * golden vectors generated from the reference's numpy backend
  * (tests/golden/make_golden.py) and against the reference tests' known answers.
  */
@@ -86,6 +86,16 @@ int orc_dg_bf_search_ref(const float *W, int N, int om, int tileSize, int nWorke
 /* Dense BF over [xBegin, xEnd) only, first `cap` minimisers in ascending order. */
 int orc_dg_bf_search_range(const float *W, int N, int om, uint64_t xBegin, uint64_t xEnd,
                            int cap, float *Emin, uint64_t *xout);
+/* Exact dense BF for integer-valued symmetric W (|sum W| < 2^30): every state
+ * in Gray-code order with integer local fields, so one state costs N integer
+ * adds and N = 32 finishes in seconds on a few cores.  For integer W the
+ * reference CPU searcher's fp32 energies are exact, so its result is the
+ * smallest min(count, tileSize) minimisers ascending: this returns the first
+ * `cap` of all minimisers ascending (Emin sign-corrected), *nMin = how many
+ * exist.  Returns the number written, -2 for bad N, -3 for non-integer,
+ * asymmetric or too large W, -4 when a worker's list overflowed. */
+int orc_dg_bf_search_exact_int(const float *W, int N, int om, int cap, int nWorkers,
+                               double *Emin, uint64_t *xout, long long *nMin);
 /* Bipartite BF with the reference CPU semantics (tile0 x tile1 tiles, up to
  * N0+N1 solutions, no sort).  xout holds (x0, x1) pairs. */
 int orc_bg_bf_search_ref(const float *b0, const float *b1, const float *W, int N0, int N1,
@@ -162,8 +172,17 @@ typedef struct orc_replay_stats {
 void orc_dg_replay(const float *h, const float *J, int N, int m, int algo,
                    uint64_t seed, uint32_t step, float G, float beta,
                    int8_t *q, const uint32_t *trace, double tol, orc_replay_stats *st);
-/* Same for the bipartite sweeps (algo: naive / coloring / sa_naive / sa_coloring). */
-void orc_bg_replay(const float *h0, const float *h1, const float *J, int N0, int N1, int m,
+/* nSteps consecutive steps (counters step0 + s, G[s], beta[s], trace of step s
+ * at trace + s * ceil(N m / 32)) with resident FP64 fields: the same decisions
+ * as orc_dg_replay at a cost that makes N = 4096, m = 256 replayable.  h and J
+ * are FP64 (the fp32 couplings of a float problem convert exactly); J must be
+ * symmetric with a zero diagonal. */
+void orc_dg_replay_steps(const double *h, const double *J, int N, int m, int algo, uint64_t seed,
+                         uint32_t step0, int nSteps, const float *G, const float *beta, int8_t *q,
+                         const uint32_t *trace, double tol, orc_replay_stats *st);
+/* Same for the bipartite sweeps (algo: naive / coloring / sa_naive / sa_coloring),
+ * with FP64 h0, h1, J. */
+void orc_bg_replay(const double *h0, const double *h1, const double *J, int N0, int N1, int m,
                    int algo, uint64_t seed, uint32_t step, float G, float beta,
                    int8_t *q0, int8_t *q1, const uint32_t *trace, double tol,
                    orc_replay_stats *st);

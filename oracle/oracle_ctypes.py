@@ -169,6 +169,21 @@ def dg_bf_search_ref(W, om=0, tile_size=1024, n_workers=0, cap=1 << 20):
     return E.value, xs[:n].copy()
 
 
+def dg_bf_search_exact_int(W, om=0, cap=1024, n_workers=0):
+    """Exact integer search of every state in Gray-code order (integer-valued
+    symmetric W only).  Returns (Emin, first `cap` minimisers ascending, count of
+    minimisers)."""
+    W = _f32(W)
+    xs = np.zeros(max(cap, 1), np.uint64)
+    E = ctypes.c_double()
+    cnt = ctypes.c_longlong()
+    n = lib().orc_dg_bf_search_exact_int(_p(W), ctypes.c_int(W.shape[0]), ctypes.c_int(om), ctypes.c_int(cap),
+                                         ctypes.c_int(n_workers), ctypes.byref(E), _p(xs), ctypes.byref(cnt))
+    if n < 0:
+        raise ValueError("orc_dg_bf_search_exact_int failed (%d)" % n)
+    return E.value, xs[:n].copy(), cnt.value
+
+
 def dg_bf_search_range(W, om, x_begin, x_end, cap):
     W = _f32(W)
     xs = np.zeros(cap, np.uint64)
@@ -316,8 +331,28 @@ def dg_replay(h, J, m, algo, seed, step, G, beta, q, trace, tol=1e-6):
     return q, st.as_dict()
 
 
+def dg_replay_steps(h, J, m, algo, seed, step0, G, beta, q, trace, tol=1e-6):
+    """len(G) consecutive dense steps with resident FP64 fields (orc_dg_replay_steps);
+    trace holds the steps' words back to back.  Returns (q after the last step, stats)."""
+    h, J = _f64(h), _f64(J)
+    q = _i8(q).copy()
+    G = _f32(np.atleast_1d(G))
+    beta = _f32(np.broadcast_to(np.asarray(beta, np.float32), G.shape))
+    trace = np.ascontiguousarray(trace, np.uint32).ravel()
+    N = len(h)
+    words = (N * m + 31) // 32
+    if trace.size < words * len(G):
+        raise ValueError("trace holds %d words, %d steps need %d" % (trace.size, len(G), words * len(G)))
+    st = ReplayStats()
+    lib().orc_dg_replay_steps(_p(h), _p(J), ctypes.c_int(N), ctypes.c_int(m), ctypes.c_int(algo),
+                              ctypes.c_uint64(seed), ctypes.c_uint32(step0), ctypes.c_int(len(G)),
+                              _p(G), _p(beta), _p(q), _p(trace), ctypes.c_double(tol), ctypes.byref(st))
+    return q, st.as_dict()
+
+
 def bg_replay(h0, h1, J, m, algo, seed, step, G, beta, q0, q1, trace, tol=1e-6):
-    h0, h1, J = _f32(h0), _f32(h1), _f32(J)
+    """One bipartite step in FP64 (h0, h1, J taken as FP64; fp32 inputs convert exactly)."""
+    h0, h1, J = _f64(h0), _f64(h1), _f64(J)
     q0, q1 = _i8(q0).copy(), _i8(q1).copy()
     trace = np.ascontiguousarray(trace, np.uint32)
     st = ReplayStats()

@@ -75,8 +75,14 @@ def optimize_flag(optimize):
         return 1
     if optimize is minimize or isinstance(optimize, Minimize):
         return 0
-    if optimize in (0, 1):
-        return int(optimize)
+    # the reference's sqaod.minimize / sqaod.maximize tags convert to 0 / 1
+    # (sqaodpy/sqaod/common/preference.py:61-62, 75-76)
+    try:
+        v = int(optimize)
+    except (TypeError, ValueError):
+        v = None
+    if v in (0, 1):
+        return v
     raise ValueError("optimize must be sqaod_gb300.minimize or sqaod_gb300.maximize")
 
 

@@ -22,22 +22,59 @@
 
 namespace sq103 {
 
+// The fixed side of a half-step, for the exact field of a flagged trial:
+// side 1 moves -> F1[y][i] = sum_j J[i][j] q0[y][j] (row i of J); side 0 moves ->
+// F0[y][j] = sum_i J[i][j] q1[y][i] (column j, stride N0).
+// The FP64 couplings of a <double> problem (J64, and h64 of the moving side) take
+// the place of the fp32 ones when present.
+struct BipFixed {
+    const float *J;
+    int N0;
+    const int8_t *qB;  // spins of the fixed side, m x NB
+    int NB;
+    int side;          // the moving side
+    float G, beta;
+    const double *J64, *h64;
+};
+
+__device__ __forceinline__ double bip_exact_field(const BipFixed &B, int y, int i) {
+    const int8_t *qb = B.qB + (size_t)y * B.NB;
+    if (B.J64)
+        return B.side ? exact_field_thread(B.J64 + (size_t)i * B.N0, 1, qb, B.NB)
+                      : exact_field_thread(B.J64 + i, (size_t)B.N0, qb, B.NB);
+    return B.side ? exact_field_thread(B.J + (size_t)i * B.N0, 1, qb, B.NB)
+                  : exact_field_thread(B.J + i, (size_t)B.N0, qb, B.NB);
+}
+
+__device__ __forceinline__ double bip_exact_h(const BipFixed &B, const float *h, int i) {
+    return B.h64 ? B.h64[i] : (double)h[i];
+}
+
 // one colour-phase trial of spin i of trotter y on the moving side; returns 1 if accepted
 __device__ __forceinline__ int bip_trial(int8_t *qA, const float *F, const float *h, int Ns, int m, int y, int i,
                                          uint64_t seed, uint32_t step, uint32_t tag, const StepConst &sc, int algo,
-                                         uint32_t *trace, unsigned long long bitBase) {
+                                         uint32_t *trace, unsigned long long bitBase, const BipFixed &B) {
     u32x4 r = draw(seed, (uint32_t)i, (uint32_t)y, step, tag);
     float u = draw_unit(r.y);
     size_t o = (size_t)y * Ns + i;
     float qyx = qA[o];
-    float dE;
-    if (algo == kSAColoring) {
+    float dE, qL = 0.f, qR = 0.f;
+    const bool sa = algo == kSAColoring;
+    if (sa) {
         dE = bip_sa_dE(qyx, h[i], F[o]);
     } else {
         int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
-        dE = bip_sqa_dE(qyx, h[i], F[o], qA[(size_t)yl * Ns + i], qA[(size_t)yr * Ns + i], sc.twoDivM, sc.coef);
+        qL = qA[(size_t)yl * Ns + i];
+        qR = qA[(size_t)yr * Ns + i];
+        dE = bip_sqa_dE(qyx, h[i], F[o], qL, qR, sc.twoDivM, sc.coef);
     }
-    if (!metropolis(dE, sc.rate, u)) return 0;
+    int nearT = 0;
+    const float L = neg_log_unit(u);
+    const DecisionTol tol = decision_tol(sa, false, sc.twoDivM, sc.coef, sc.rate);
+    int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[i], F[o], L), nearT);
+    if (nearT)
+        acc = exact_accept(sa, false, qyx, bip_exact_h(B, h, i), bip_exact_field(B, y, i), qL, qR, m, B.G, B.beta, u);
+    if (!acc) return 0;
     qA[o] = (int8_t)(-qyx);
     if (trace) {
         unsigned long long bit = bitBase + o;
@@ -50,14 +87,17 @@ __global__ void __launch_bounds__(256) bip_flip_phase(int8_t *qA, const float *F
                                                       int yb, int ys, int cnt, uint64_t seed, uint32_t step,
                                                       uint32_t tag, const float *Gp, const float *bp, float Gsc, float bsc,
                                                       int algo, uint32_t *trace, unsigned long long bitBase,
-                                                      unsigned long long *accepted) {
+                                                      unsigned long long *accepted, BipFixed B) {
     long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool active = idx < (long long)cnt * Ns;
     int acc = 0;
     if (active) {
-        StepConst sc = step_const(algo, m, Gp ? *Gp : Gsc, bp ? *bp : bsc);
+        const float G = Gp ? *Gp : Gsc, beta = bp ? *bp : bsc;
+        StepConst sc = step_const(algo, m, G, beta);
         int t = (int)(idx / Ns), i = (int)(idx - (long long)t * Ns);
-        acc = bip_trial(qA, F, h, Ns, m, yb + t * ys, i, seed, step, tag, sc, algo, trace, bitBase);
+        B.G = G;
+        B.beta = beta;
+        acc = bip_trial(qA, F, h, Ns, m, yb + t * ys, i, seed, step, tag, sc, algo, trace, bitBase, B);
     }
     if (accepted) {
         unsigned ballot = __ballot_sync(0xffffffffu, acc);
@@ -130,7 +170,20 @@ __global__ void __launch_bounds__(256) bip_naive(sq103_bipartite_task T, int s) 
                 dE = bip_sqa_dE(qyx, h[x], F, qA[(size_t)yl * Ns + x], qA[(size_t)yr * Ns + x], sc.twoDivM,
                                 sc.coef);
             }
-            if (metropolis(dE, sc.rate, su)) {
+            int nearT = 0;
+            const float L = neg_log_unit(su);
+            const DecisionTol tol = decision_tol(sa, false, sc.twoDivM, sc.coef, sc.rate);
+            int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[x], F, L), nearT);
+            if (nearT) {
+                const int NB = side ? T.N0 : T.N1;
+                const BipFixed B = {T.J, T.N0, side ? T.q0 : T.q1, NB, side, 0.f, 0.f, T.J64,
+                                    side ? T.h1_64 : T.h0_64};
+                const float qL = sa ? 0.f : qA[(size_t)(y == 0 ? T.m - 1 : y - 1) * Ns + x];
+                const float qR = sa ? 0.f : qA[(size_t)(y == T.m - 1 ? 0 : y + 1) * Ns + x];
+                acc = exact_accept(sa, false, qyx, bip_exact_h(B, h, x), bip_exact_field(B, y, x), qL, qR, T.m,
+                                   T.G ? T.G[s] : T.Gs, T.beta ? T.beta[s] : T.betas, su);
+            }
+            if (acc) {
                 qA[(size_t)y * Ns + x] = (int8_t)(-qyx);
                 ++accepted;
                 if (T.trace) {
@@ -188,6 +241,9 @@ __global__ void __launch_bounds__(256) bip_batch_persistent(const sq103_bipartit
                                                                 tx, smem);
                     }
                 const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
+                const BipFixed B = {T.J, T.N0, side ? T.q0 : T.q1, side ? T.N0 : T.N1, side,
+                                    T.G ? T.G[s] : T.Gs, T.beta ? T.beta[s] : T.betas, T.J64,
+                                    side ? T.h1_64 : T.h0_64};
                 for (int ph = 0; ph < 3; ++ph) {
                     int yb, ys, cnt;
                     if (sa) {
@@ -203,7 +259,8 @@ __global__ void __launch_bounds__(256) bip_batch_persistent(const sq103_bipartit
                     }
                     for (long long k = threadIdx.x; k < (long long)cnt * Ns; k += blockDim.x) {
                         int t = (int)(k / Ns), i = (int)(k - (long long)t * Ns);
-                        accepted += bip_trial(qA, F, h, Ns, m, yb + t * ys, i, T.seed, step, tag, sc, T.algo, nullptr, 0);
+                        accepted += bip_trial(qA, F, h, Ns, m, yb + t * ys, i, T.seed, step, tag, sc, T.algo, nullptr, 0,
+                                              B);
                     }
                     __syncthreads();
                 }
@@ -262,7 +319,16 @@ extern "C" SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task
             int8_t *qA = side ? T.q1 : T.q0;
             float *F = side ? T.F1 : T.F0;
             const float *h = side ? T.h1 : T.h0;
-            sq103_bipartite_fields(T.J, T.N0, T.N1, side ? T.q0 : T.q1, side, F, m, stream);
+            if (T.digits1 && T.digits0) {
+                // side 1: F1 = q0 J^T (rows of J, K = N0); side 0: F0 = q1 J (rows of J^T, K = N1)
+                const int rc = side ? sq103_tc_refresh(T.digits1, T.N1, T.N0, T.q0, T.N0, m, T.spinsBf16, F, T.N1,
+                                                       0, T.status, stream)
+                                    : sq103_tc_refresh(T.digits0, T.N0, T.N1, T.q1, T.N1, m, T.spinsBf16, F, T.N0,
+                                                       0, T.status, stream);
+                if (rc != 0) return rc;
+            } else {
+                sq103_bipartite_fields(T.J, T.N0, T.N1, side ? T.q0 : T.q1, side, F, m, stream);
+            }
             const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
             for (int ph = 0; ph < 3; ++ph) {
                 int yb, ys, cnt;
@@ -282,8 +348,10 @@ extern "C" SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task
                 bip_flip_phase<<<(int)((n + 255) / 256), 256, 0, st>>>(qA, F, h, Ns, m, yb, ys, cnt, T.seed, step, tag,
                                                                        T.G ? T.G + s : nullptr,
                                                                        T.beta ? T.beta + s : nullptr, T.Gs, T.betas,
-                                                                       T.algo, trace, bitBase,
-                                                                       T.accepted);
+                                                                       T.algo, trace, bitBase, T.accepted,
+                                                                       BipFixed{T.J, T.N0, side ? T.q0 : T.q1,
+                                                                                side ? T.N0 : T.N1, side, 0.f, 0.f,
+                                                                                T.J64, side ? T.h1_64 : T.h0_64});
             }
             bitBase += (unsigned long long)m * Ns;
         }

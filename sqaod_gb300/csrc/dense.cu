@@ -57,6 +57,17 @@ __device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F,
     }
 }
 
+// The FP64 decision of a flagged trial at site x of a trotter whose spins are
+// qy: from the exact field over the FP64 couplings of a <double> problem when
+// the task has them, else over the fp32 couplings.
+__device__ __forceinline__ int exact_dense_accept(const sq103_dense_task &T, bool sa, int x, float qyx,
+                                                  const int8_t *qy, float qL, float qR, float G, float beta, float u) {
+    const double F = T.J64 ? exact_field_thread(T.J64 + (size_t)x * T.N, 1, qy, T.N)
+                           : exact_field_thread(T.J + (size_t)x * T.ldJ, 1, qy, T.N);
+    const double hx = T.h64 ? T.h64[x] : (double)T.h[x];
+    return exact_accept(sa, true, qyx, hx, F, qL, qR, T.m, G, beta, u);
+}
+
 // Dynamic shared memory every launch of anneal_instance needs: the flip lists
 // of two phases (2 m entries) and their counters, rounded to 16 bytes.
 __host__ __device__ constexpr size_t flip_list_bytes(int m) {
@@ -111,6 +122,7 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
     for (int s = s0; s < s0 + nSteps; ++s) {
         const float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
         const StepConst sc = step_const(T.algo, m, G, beta);
+        const DecisionTol tol = decision_tol(T.algo == kSANaive, true, sc.twoDivM, sc.coef, sc.rate);
         const uint32_t step = T.step0 + (uint32_t)s;
         uint32_t *trace = T.trace ? T.trace + (size_t)(s - s0) * wordsPerStep : nullptr;
 
@@ -124,9 +136,12 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
                     size_t o = (size_t)y * N + x;
                     float qyx = q[o];
                     int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
-                    float dE = dense_sqa_dE(qyx, h[x], F[o], q[(size_t)yl * N + x], q[(size_t)yr * N + x],
-                                            sc.twoDivM, sc.coef);
-                    int acc = metropolis(dE, sc.rate, u);
+                    const float qL = q[(size_t)yl * N + x], qR = q[(size_t)yr * N + x];
+                    float dE = dense_sqa_dE(qyx, h[x], F[o], qL, qR, sc.twoDivM, sc.coef);
+                    int nearT = 0;
+                    const float L = neg_log_unit(u);
+                    int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[x], __fmul_rn(2.f, F[o]), L), nearT);
+                    if (nearT) acc = exact_dense_accept(T, false, x, qyx, q + (size_t)y * N, qL, qR, G, beta, u);
                     if (acc) {
                         q[o] = (int8_t)(-qyx);
                         naiveFlip = Flip{y, x, -2.f * qyx};
@@ -166,15 +181,22 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
                     float u = draw_unit(r.y);
                     size_t o = (size_t)y * N + x;
                     float qyx = q[o];
-                    float dE;
+                    float dE, qL = 0.f, qR = 0.f;
                     if (sa) {
                         dE = dense_sa_dE(qyx, h[x], F[o]);
                     } else {
                         int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
-                        dE = dense_sqa_dE(qyx, h[x], F[o], q[(size_t)yl * N + x], q[(size_t)yr * N + x],
-                                          sc.twoDivM, sc.coef);
+                        qL = q[(size_t)yl * N + x];
+                        qR = q[(size_t)yr * N + x];
+                        dE = dense_sqa_dE(qyx, h[x], F[o], qL, qR, sc.twoDivM, sc.coef);
                     }
-                    if (metropolis(dE, sc.rate, u)) {
+                    // trials of one phase are independent: the row of trotter y holds every
+                    // earlier flip of y, so its exact field is the one this trial sees
+                    int nearT = 0;
+                    const float L = neg_log_unit(u);
+                    int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[x], __fmul_rn(2.f, F[o]), L), nearT);
+                    if (nearT) acc = exact_dense_accept(T, sa, x, qyx, q + (size_t)y * N, qL, qR, G, beta, u);
+                    if (acc) {
                         q[o] = (int8_t)(-qyx);
                         int slot = atomicAdd(&nflip[buf], 1);
                         fl[slot] = Flip{y, x, -2.f * qyx};
@@ -312,8 +334,9 @@ SQ103_API int sq103_dense_anneal(const sq103_dense_task *task, void *stream) {
     if (task->nSteps == 0) return 0;
     // one CTA per trotter when the shape allows it (or when asked to), else one CTA
     const bool rowsAligned = !(task->ldJ & 3) && !(reinterpret_cast<uintptr_t>(task->J) & 15);
-    bool multi = task->flags == 2 ||
-                 (task->flags == 0 && task->ws && rowsAligned &&
+    const int kernel = task->flags & kFlagKernelMask;
+    bool multi = kernel == 2 ||
+                 (kernel == 0 && task->ws && rowsAligned &&
                   task->wsBytes >= sq103_dense_ws_bytes(task->N, task->m, task->nSteps) &&
                   sq103_dense_multicta_ok(task->N, task->m, task->algo));
     if (multi) {

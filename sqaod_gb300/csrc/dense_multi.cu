@@ -71,6 +71,7 @@ constexpr int kCand = 2;        // neighbour iterations per lane and batch found
 constexpr int kPredRows = 8;    // predicted accepting lanes whose gathers are kept in registers
 constexpr float kFieldDrift = 1.f;  // assumed field change between prefetch and decision
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;
+constexpr unsigned long long kShortWaitNs = 1000000ull;  // task flag kFlagShortWaits (tests)
 // the prefetchers run ahead and mostly wait: they poll gently, which leaves the
 // SM's shared load/store path to the decider
 constexpr int kPrefetchSleepNs = 128;
@@ -132,6 +133,11 @@ struct McShared {
     volatile int decDone;                  // batches [0, decDone) no longer read from the buffers (decider)
     volatile int done;
     int nflip;
+    // exact decisions (rare): the decider posts a trial, the helper warp answers
+    volatile int exReq;    // number of the latest request (decider)
+    volatile int exDone;   // number of the latest answer (helper)
+    int exX, exBits;       // the trial's site; its FP64 outcomes for qL + qR = -2, 0, +2 (bits 0-2)
+    float exQ, exU, exG, exBeta;
 };
 
 // every lane loads the flag with acquire semantics (one broadcast access); the
@@ -144,11 +150,11 @@ __device__ __forceinline__ int avail_of(unsigned long long v, int n) { return (i
 
 // bounded wait on a warp-uniform condition; false on timeout
 template <int SLEEP_NS = 32, class F>
-__device__ __forceinline__ bool wait_until(F &&ready) {
+__device__ __forceinline__ bool wait_until(unsigned long long limitNs, F &&ready) {
     unsigned long long t0 = 0;
     while (!ready()) {
         if (t0 == 0) t0 = global_ns();
-        if (global_ns() - t0 > kWaitLimitNs) return false;
+        if (global_ns() - t0 > limitNs) return false;
         __nanosleep(SLEEP_NS);
     }
     return true;
@@ -250,13 +256,18 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
     const int nWG = (N + 31) / 32;
     const int ghostStride = (nWG + 1) & ~1;
     const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
+    // test hooks (task flags): every wait gives up after 1 ms; trotter 0 never
+    // publishes its accept words, so its neighbours' waits run out
+    const unsigned long long waitNs = (T.flags & kFlagShortWaits) ? kShortWaitNs : kWaitLimitNs;
+    const bool publish = !((T.flags & kFlagWithholdTrotter0) && y == 0);
 
     float *Fs = reinterpret_cast<float *>(smem);                        // N
     float *hs = Fs + N;                                                 // N
     float *Jg = hs + N;                                                 // kPre x 32 x 33
     float *preU = Jg + kPre * kJgStride;                                // kPre x 32
     float *preC = preU + kPre * 32;                                     // kPre x 3 x 32
-    int *preX = reinterpret_cast<int *>(preC + kPre * 96);              // kPre x 32
+    float *preL = preC + kPre * 96;                                     // kPre x 32: -ln u
+    int *preX = reinterpret_cast<int *>(preL + kPre * 32);              // kPre x 32
     uint32_t *ghost = reinterpret_cast<uint32_t *>(preX + kPre * 32);   // 2 x ghostStride
     uint32_t *bm = ghost + 2 * ghostStride;                             // 2 x kBmSlots x kBmWords
     int *ring = reinterpret_cast<int *>(bm + 2 * kBmSlots * kBmWords);  // 2 x kRing
@@ -280,6 +291,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         }
     }
     if (tid == 0) {
+        S.exReq = S.exDone = 0;
         S.logAvail = 0;
         S.applied[0] = S.applied[1] = 0;
         for (int i = 0; i < kPre; ++i) S.readyTag[i] = 0;
@@ -304,6 +316,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         for (int t = 0; t < kGv; ++t) gv[t] = 0.f;
 
         int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
+        int exSeq = 0;       // exact-decision requests posted to the helper warp
 
         // Applies the published neighbour iterations below lim0 / lim1 (their sites
         // are in the ring) to the ghost rows; returns the helper's availability word.
@@ -390,7 +403,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             }
         };
 
-        aborted = !wait_until([&] { return uniform_acquire(&S.readyTag[0]) == 1; });
+        aborted = !wait_until(waitNs, [&] { return uniform_acquire(&S.readyTag[0]) == 1; });
         x = preX[lane];
         float Fv = Fs[x];
 
@@ -399,7 +412,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             const int buf = b & (kPre - 1);
             const int nValid = min(32, Itot - g0);
             const bool valid = lane < nValid;
-            const float u = preU[buf * 32 + lane];
+            const float u = preU[buf * 32 + lane], Lu = preL[buf * 32 + lane];
             const StepConst sc = {preC[buf * 96 + lane], preC[buf * 96 + 32 + lane], preC[buf * 96 + 64 + lane]};
             const float *jg = Jg + buf * kJgStride + lane * 33;
             const unsigned pred = prePred[buf];  // lanes whose row of in-batch gathers is in jg
@@ -426,7 +439,12 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             // decide the batch in rounds
             unsigned pending = __ballot_sync(FULL, valid), accBits = 0;
             float d = 0.f;
+            bool exValid = false;  // exBits holds the FP64 outcomes of the lane's trial
+            int exBits = 0;
+            int exLane = -1;       // a flagged lane whose trial waits for its exact decision
+            const DecisionTol tolD = decision_tol(sa, true, sc.twoDivM, sc.coef, sc.rate);
             bool evalNbr = nNbr > 0;  // (one instance of nbr_bits keeps the loop's code small)
+            for (;;) {
             while (pending) {
                 if (evalNbr) {
                     nbr_bits(b, g0, valid, avEval);
@@ -434,14 +452,18 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                     evalNbr = false;
                 }
                 // a lane with unknown neighbour bits is decided anyway when every value
-                // those bits can take gives the same outcome; it blocks otherwise
-                int acc = 0, amb = 0;
+                // those bits can take gives the same outcome; it blocks otherwise.  The
+                // outcomes come from the fp32 field, flagged where its rounding could
+                // change them, or from the FP64 outcomes of a flagged lane's trial
+                int acc = 0, amb = 0, nearT = 0;
                 if ((pending >> lane) & 1u) {
                     const float qn0 = qb0 ? 1.f : -1.f, qn1 = nNbr == 1 ? qn0 : (qb1 ? 1.f : -1.f);
-                    auto accept = [&](float a, float c) {
+                    const float xt = trial_xtol(tolD, hx, __fmul_rn(2.f, Fv), Lu);
+                    auto accept = [&](float a, float c) -> int {
+                        if (exValid) return (exBits >> (((int)a + (int)c + 2) >> 1)) & 1;
                         const float dE = sa ? dense_sa_dE(qx, hx, Fv)
                                             : dense_sqa_dE(qx, hx, Fv, a, c, sc.twoDivM, sc.coef);
-                        return (int)metropolis(dE, sc.rate, u);
+                        return metropolis_log(dE, sc.rate, Lu, xt, nearT);
                     };
                     acc = accept(qn0, qn1);
                     if ((blocked >> lane) & 1u) {
@@ -453,15 +475,25 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 }
                 const unsigned accM = __ballot_sync(FULL, acc && !amb) & pending;
                 const unsigned blkM = __ballot_sync(FULL, amb) & pending;
+                const unsigned nearM = __ballot_sync(FULL, nearT) & pending;
+                if (nearM) {
+                    // a flagged lane that would be this round's first decision needs its
+                    // exact decision first (served below, outside the rounds)
+                    const int fl = __ffs(accM | blkM | nearM) - 1;
+                    if ((nearM >> fl) & 1u) {
+                        exLane = fl;
+                        break;
+                    }
+                }
                 const int fa = accM ? __ffs(accM) - 1 : 32;
                 const int fb = blkM ? __ffs(blkM) - 1 : 32;
                 if (fb < fa) {
                     // undecided lanes below fb reject; fb waits for its neighbour trials
                     pending &= ~((1u << fb) - 1u);
-                    if (lane == 0) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fb, accBits));
+                    if (lane == 0 && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fb, accBits));
                     const int w0 = __shfl_sync(FULL, nd0, fb), w1 = __shfl_sync(FULL, nd1, fb);
                     unsigned long long av = 0;
-                    if (!wait_until([&] {
+                    if (!wait_until(waitNs, [&] {
                             av = uniform_acquire64(&S.logAvail);
                             return avail_of(av, 0) > w0 && (nNbr < 2 || avail_of(av, 1) > w1);
                         })) {
@@ -490,17 +522,43 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                     const float jv = ((pred >> fa) & 1u) ? jg[fa] : __ldg(T.J + (size_t)xf * T.ldJ + x);
                     Fv = __fmaf_rn(df, jv, Fv);
                     if (x == xf) qx = -qx;
+                    exValid = false;  // the trial now follows another flip
                 }
                 accBits |= 1u << fa;
                 pending &= ~((2u << fa) - 1u);
                 // trials through fa are decided: make them visible to the neighbours
-                if (lane == 0 && pending) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
+                if (lane == 0 && pending && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
+            }
+            if (exLane < 0 || aborted) break;
+            // The flagged lane's FP64 outcomes for each value of its neighbours' sum,
+            // computed by the helper warp from the exact field (every flip before the
+            // trial is in qs); the rounds then resume where they stopped.
+            if (lane == exLane) {
+                const int sl = (g0 + lane) / N;
+                S.exX = x;
+                S.exQ = qx;
+                S.exU = u;
+                S.exG = T.G ? T.G[sl] : T.Gs;
+                S.exBeta = T.beta ? T.beta[sl] : T.betas;
+            }
+            ++exSeq;
+            __syncwarp();
+            if (lane == 0) st_release_cta(&S.exReq, exSeq);
+            if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) {
+                aborted = true;
+                break;
+            }
+            if (lane == exLane) {
+                exBits = S.exBits;
+                exValid = true;
+            }
+            exLane = -1;
             }
             if (aborted) break;
             __syncwarp();
             if (lane == 0) {
                 S.decDone = b + 1;  // this batch's buffer is free
-                st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, nValid, accBits));
+                if (publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, nValid, accBits));
             }
             const int nf = __popc(accBits);
             accepted += (unsigned long long)nf;
@@ -509,7 +567,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             const bool more = b + 1 < nBatches;
             // (while waiting, keep applying published neighbour iterations of this and
             // earlier batches: the prefetchers may need those ring slots)
-            if (more && !wait_until([&] {
+            if (more && !wait_until(waitNs, [&] {
                     if (uniform_acquire(&S.readyTag[(b + 1) & (kPre - 1)]) == b + 2) return true;
                     if (nNbr > 0) apply_nbr(g0 + 32, g0 + 32);
                     return false;
@@ -568,10 +626,36 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
     } else if (warp == 1) {
         // -------------------------------------------------------------- helper
         // lane l < 4 polls word (avail[n] >> 5) + dw of neighbour n = l & 1, dw = l >> 1
-        int avail0 = 0, avail1 = 0;
+        int avail0 = 0, avail1 = 0, served = 0;
         const int n = lane & 1, dw = lane >> 1;
         const unsigned long long *nbLog = outLog + (size_t)(n ? nbr1 : nbr0) * nWords;
-        while (nNbr > 0 && !__shfl_sync(FULL, (int)S.done, 0)) {
+        while (!__shfl_sync(FULL, (int)S.done, 0)) {
+            // an exact decision the decider waits for: the trial's exact field (the
+            // integer row sum, as the one-CTA kernel computes it) and its FP64 outcome
+            // for each value of the neighbours' sum
+            const int req = uniform_acquire(&S.exReq);
+            if (req != served) {
+                served = req;
+                const int xr = S.exX;
+                const float qr = S.exQ, ur = S.exU, Gr = S.exG, br = S.exBeta;
+                const double hr = T.h64 ? T.h64[xr] : (double)hs[xr];
+                const double F = T.J64 ? exact_field_warp(T.J64 + (size_t)xr * N, qs, N)
+                                       : exact_field_warp(T.J + (size_t)xr * T.ldJ, qs, N);
+                if (lane == 0) {
+                    int bits = 0;
+                    for (int k = 0; k < 3; ++k) {
+                        const float qL = k == 0 ? -1.f : 1.f, qR = k == 2 ? 1.f : -1.f;  // sum -2, 0, +2
+                        bits |= exact_accept(sa, true, qr, hr, F, qL, qR, m, Gr, br, ur) << k;
+                    }
+                    S.exBits = bits;
+                    st_release_cta(&S.exDone, req);
+                }
+                __syncwarp();
+            }
+            if (nNbr == 0) {
+                __nanosleep(64);
+                continue;
+            }
             const int an = n ? avail1 : avail0;
             const int w = (an >> 5) + dw;
             unsigned long long v = 0;
@@ -616,7 +700,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             // and ring slots j - kRing are applied for the neighbours' iterations j of batch p
             const int jEnd = 32 * p + 32;
             int stop = 0;
-            if (!wait_until<kPrefetchSleepNs>([&] {
+            if (!wait_until<kPrefetchSleepNs>(waitNs, [&] {
                     int ok = 0;
                     if (lane == 0) {
                         stop = S.done;
@@ -657,7 +741,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 float qn1 = nNbr > 1 ? (((vg[ghostStride + (x >> 5)] >> (x & 31)) & 1u) ? 1.f : -1.f) : qn0;
                 const float dE = sa ? dense_sa_dE(qx, hx, fx) : dense_sqa_dE(qx, hx, fx, qn0, qn1, sc.twoDivM, sc.coef);
                 const float margin = (sa ? 4.f : 2.f * sc.twoDivM) * kFieldDrift;
-                pred = __ballot_sync(FULL, valid && metropolis(dE - margin, sc.rate, u));
+                const float dEm = dE - margin;
+                pred = __ballot_sync(FULL, valid && (dEm < 0.f || __fmul_rn(dEm, sc.rate) < neg_log_unit(u)));
             }
             float v[kPredRows];
             {
@@ -697,7 +782,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 }
                 // batch p - 1 (the other prefetcher's) must be in the ring; its buffer
                 // slot may already hold a later batch (batch p - 2 is this warp's own)
-                if (p > 0 && !wait_until<kPrefetchSleepNs>([&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
+                if (p > 0 && !wait_until<kPrefetchSleepNs>(waitNs, [&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
                     break;
                 __syncwarp();
                 const int hb = x & (kBmBits - 1);
@@ -764,6 +849,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             if (lane == 0) prePred[buf] = pred;
             preX[buf * 32 + lane] = x;
             preU[buf * 32 + lane] = u;
+            preL[buf * 32 + lane] = neg_log_unit(u);
             preC[buf * 96 + lane] = sc.twoDivM;
             preC[buf * 96 + 32 + lane] = sc.coef;
             preC[buf * 96 + 64 + lane] = sc.rate;
@@ -837,7 +923,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
 
 static size_t multi_smem_bytes(int N) {
     size_t ghostStride = (size_t)((N + 31) / 32 + 1) & ~(size_t)1;
-    return (size_t)N * 4 * 2 + (size_t)kPre * (kJgStride + 32 + 96 + 32) * 4 + 2 * ghostStride * 4 +
+    return (size_t)N * 4 * 2 + (size_t)kPre * (kJgStride + 32 + 96 + 32 + 32) * 4 + 2 * ghostStride * 4 +
            (size_t)2 * kBmSlots * kBmWords * 4 + 2 * kRing * 4 + 2 * kLogWords * 4 + (size_t)kPre * 2 * kCand * 32 * 4 + kPre * 4 +
            32 * 8 + (size_t)N + 16;
 }

@@ -305,8 +305,16 @@ SQ103_API int sq103_dense_energy_static(const float *J, int ldJ, const float *h,
     }
     double *scratch = nullptr;
     int rc = static_scratch(&scratch);
+    if (rc == kErrBadShape) {
+        sq103_set_error("sq103_dense_energy_static: the current device number is 256 or more; the static "
+                        "scratch addresses are kept for devices 0-255 only.");
+        return rc;
+    }
     if (rc != 0) {
-        sq103_set_error("sq103_dense_energy_static: cudaGetSymbolAddress of the static scratch failed.");
+        char msg[160];
+        snprintf(msg, sizeof(msg), "sq103_dense_energy_static: looking up the static scratch failed: %s.",
+                 cudaGetErrorString((cudaError_t)rc));
+        sq103_set_error(msg);
         return rc;
     }
     return sq103_dense_energy(J, ldJ, h, c64, q, N, m, maximize, scratch, E64, E32, stream);

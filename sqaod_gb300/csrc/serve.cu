@@ -116,6 +116,10 @@ public:
         sq103_dense_task dt = {};
         sq103_bipartite_task bt = {};
         double *c64 = nullptr;
+        int *dStatus = nullptr;        // this request's own timeout status word (dense sweeps)
+        void *digits = nullptr;        // tensor-core refresh of a dense request with N >= 1024
+        void *spinsBf16 = nullptr;
+        int status = 0;                // its value once the request is done
         // results
         std::vector<double> E;
         std::vector<int8_t> q0, q1;
@@ -128,9 +132,7 @@ public:
         bPos_.ensure(maxSlots);
         counts_.ensure(2);
         queues_.ensure(4);
-        status_.ensure(1);
         stage_.init((size_t)96 << 20);
-        SQ_CHECK(cudaMemsetAsync(status_.p, 0, sizeof(int), st_.get()));
         SQ_CHECK(cudaMemsetAsync(queues_.p, 0, sizeof(int) * 4, st_.get()));
         SQ_CHECK(cudaMemsetAsync(counts_.p, 0, sizeof(int) * 2, st_.get()));
         int dev = 0;
@@ -234,7 +236,8 @@ public:
             if (r->pos >= r->nSteps) continue;  // finishing: its results are being collected
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)
-                SQ_CHECK(sq103_dense_field_refresh(r->dt.J, r->dt.ldJ, r->dt.q, r->dt.F, r->N0, r->m, st_.get()));
+                SQ_CHECK(sq103_dense_refresh(r->dt.J, r->dt.ldJ, r->digits, r->spinsBf16, r->dt.q, r->dt.F, r->N0,
+                                             r->m, r->dStatus, st_.get()));
             if (r->pos >= r->nSteps) finished.push_back(r);
         }
         for (Request *r : finished) finish(r);
@@ -270,6 +273,17 @@ public:
         for (int i = 0; i < n; ++i) ids[i] = completed_[i];
         completed_.erase(completed_.begin(), completed_.begin() + n);
         return n;
+    }
+
+    // Fault injection from the host (tests): writes `value` into an active dense
+    // request's status word, in stream order, as a sweep that gave up a bounded
+    // wait would.  Only that request then reports the error.
+    void injectStatus(int id, int value) {
+        auto it = all_.find(id);
+        throwErrorIf(it == all_.end(), "unknown request id %d.", id);
+        Request *r = it->second.get();
+        throwErrorIf(r->state != kActive || r->dStatus == nullptr, "request %d is not an active request.", id);
+        stage_.copy(r->dStatus, &value, sizeof(int), st_.get());
     }
 
     void setLargeLimit(int n) {
@@ -311,10 +325,15 @@ private:
         if (r.kind == 0) {
             size_t N = r.N0, m = r.m;
             s += al(N * ldj(N) * 4) + al(N * 4) + al(m * N * 4) + al(m * N) + al(m * N * 8);
+            if (sq103_dense_refresh_uses_tc((int)N))
+                s += al(sq103_tc_digits_bytes((int)N, (int)N)) + al(sq103_tc_spins_bytes((int)m, (int)N));
         } else {
             size_t N0 = r.N0, N1 = r.N1, m = r.m;
             s += al(N0 * N1 * 4) + al(N0 * 4) + al(N1 * 4) + al(m * N0) + al(m * N1) + al(m * N0 * 4) +
                  al(m * N1 * 4) + al(m * N1 * 8);
+            if (sq103_bipartite_refresh_uses_tc((int)N0, (int)N1))
+                s += al(sq103_tc_digits_bytes((int)N1, (int)N0)) + al(sq103_tc_digits_bytes((int)N0, (int)N1)) +
+                     al(sq103_tc_spins_bytes((int)m, (int)std::max(N0, N1)));
         }
         return s;
     }
@@ -332,8 +351,11 @@ private:
         size_t i = 0;
         while (i < queue_.size()) {
             Request *r = queue_[i];
+            // bipartite requests whose fields the single-instance annealer computes on the
+            // tensor cores take the per-instance kernels, which do the same
             const bool large = r->kind == 0 ? !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring)
-                                            : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork;
+                                            : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork ||
+                                                  sq103_bipartite_refresh_uses_tc(r->N0, r->N1);
             const bool fits =
                 used_ + r->bytes <= budget_ &&
                 (large ? (int)large_.size() < maxLarge_  // each steps with the whole GPU every tick
@@ -362,17 +384,23 @@ private:
         if (r->kind == 0) {
             const size_t N = r->N0;
             const size_t ldJ = ldj(N);  // rows padded to 16 bytes for the one-CTA-per-trotter sweep
+            const bool tc = sq103_dense_refresh_uses_tc((int)N);  // as the single-instance annealer
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh = oJ + al(N * ldJ * 4), oc = oh + al(N * 4),
                    oF = oc + 512, oq = oF + al(m * N * 4), oR = oq + al(m * N), oE = oR + al(m * N * 8),
-                   oWs = oE + al(m * 8),
+                   oD = oE + al(m * 8), oA = oD + (tc ? al(sq103_tc_digits_bytes((int)N, (int)N)) : 0),
+                   oWs = oA + (tc ? al(sq103_tc_spins_bytes(m, (int)N)) : 0),
                    tot = oWs + (r->large ? al(sq103_dense_ws_bytes((int)N, m, kStepsPerTick)) : 0);
             r->bytes += tot - oWs;  // the accept-word workspace of a large instance
             r->mem.alloc(tot, st_.get());
+            r->digits = tc ? r->mem.p + oD : nullptr;
+            r->spinsBf16 = tc ? r->mem.p + oA : nullptr;
             unsigned char *b = r->mem.p;
             r->dE = (double *)(b + oE);
             float *G = (float *)(b + oG), *beta = (float *)(b + oB), *J = (float *)(b + oJ), *h = (float *)(b + oh);
             float *c32 = (float *)(b + oc);
             r->c64 = (double *)(b + oc + 256);
+            r->dStatus = (int *)(b + oc + 384);
+            SQ_CHECK(cudaMemsetAsync(r->dStatus, 0, sizeof(int), st_.get()));
             float *F = (float *)(b + oF);
             int8_t *q = (int8_t *)(b + oq);
             double *scratch = (double *)(b + oR);  // N doubles for the hamiltonian, m N for energies
@@ -383,15 +411,17 @@ private:
             SQ_CHECK(cudaMemsetAsync(J, 0, sizeof(float) * N * ldJ, st_.get()));
             SQ_CHECK(sq103_dense_hamiltonian(dW_.p, (int)N, (int)N, r->optimize, h, J, (int)ldJ, c32, r->c64, scratch,
                                              st_.get()));
+            if (r->digits) SQ_CHECK(sq103_tc_make_digits(J, (int)ldJ, (int)N, (int)N, 0, r->digits, st_.get()));
             SQ_CHECK(sq103_randomize_spins(q, (int)N, m, r->seed, 0, 0, st_.get()));
-            SQ_CHECK(sq103_dense_field_refresh(J, (int)ldJ, q, F, (int)N, m, st_.get()));
+            SQ_CHECK(sq103_dense_refresh(J, (int)ldJ, r->digits, r->spinsBf16, q, F, (int)N, m, r->dStatus,
+                                         st_.get()));
             sq103_dense_task &t = r->dt;
             t = sq103_dense_task{};
             t.J = J; t.h = h; t.q = q; t.F = F; t.G = G; t.beta = beta;
             t.seed = r->seed; t.step0 = 1; t.N = (int)N; t.m = m; t.ldJ = (int)ldJ;
             t.algo = m == 1 ? kSANaive : kColoring;
             t.nSteps = n;
-            t.status = status_.p;
+            t.status = r->dStatus;
             if (r->large) {
                 t.ws = b + oWs;  // its own: large instances step together in packed launches
                 t.wsBytes = sq103_dense_ws_bytes((int)N, m, kStepsPerTick);
@@ -405,10 +435,13 @@ private:
             }
         } else {
             const size_t N0 = r->N0, N1 = r->N1;
+            const bool tc = sq103_bipartite_refresh_uses_tc((int)N0, (int)N1);  // as the single-instance annealer
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh0 = oJ + al(N0 * N1 * 4), oh1 = oh0 + al(N0 * 4),
                    oc = oh1 + al(N1 * 4), oq0 = oc + 512, oq1 = oq0 + al(m * N0), oF0 = oq1 + al(m * N1),
                    oF1 = oF0 + al(m * N0 * 4), oR = oF1 + al(m * N1 * 4), oE = oR + al(std::max(m * N1, N0 + N1) * 8),
-                   tot = oE + al(m * 8);
+                   oD1 = oE + al(m * 8), oD0 = oD1 + (tc ? al(sq103_tc_digits_bytes((int)N1, (int)N0)) : 0),
+                   oA = oD0 + (tc ? al(sq103_tc_digits_bytes((int)N0, (int)N1)) : 0),
+                   tot = oA + (tc ? al(sq103_tc_spins_bytes(m, (int)std::max(N0, N1))) : 0);
             r->mem.alloc(tot, st_.get());
             unsigned char *b = r->mem.p;
             r->dE = (double *)(b + oE);
@@ -428,9 +461,21 @@ private:
                                                  r->optimize, h0, h1, J, c32, r->c64, scratch, st_.get()));
             SQ_CHECK(sq103_randomize_spins(q0, (int)N0, m, r->seed, 0, 0, st_.get()));
             SQ_CHECK(sq103_randomize_spins(q1, (int)N1, m, r->seed, 0, 1, st_.get()));
+            r->dStatus = (int *)(b + oc + 384);
+            SQ_CHECK(cudaMemsetAsync(r->dStatus, 0, sizeof(int), st_.get()));
+            if (tc) {
+                SQ_CHECK(sq103_tc_make_digits(J, (int)N0, (int)N1, (int)N0, 0, b + oD1, st_.get()));
+                SQ_CHECK(sq103_tc_make_digits(J, (int)N0, (int)N0, (int)N1, 1, b + oD0, st_.get()));
+            }
             sq103_bipartite_task &t = r->bt;
             t = sq103_bipartite_task{};
             t.J = J; t.h0 = h0; t.h1 = h1; t.q0 = q0; t.q1 = q1; t.F0 = F0; t.F1 = F1;
+            if (tc) {
+                t.digits1 = b + oD1;
+                t.digits0 = b + oD0;
+                t.spinsBf16 = b + oA;
+            }
+            t.status = r->dStatus;
             t.G = G; t.beta = beta; t.seed = r->seed; t.step0 = 1;
             t.N0 = (int)N0; t.N1 = (int)N1; t.m = m;
             t.algo = m == 1 ? kSAColoring : kColoring;
@@ -505,8 +550,10 @@ private:
                 SQ_CHECK(cudaMemcpyAsync(r->q1.data(), r->bt.q1, r->q1.size(), cudaMemcpyDeviceToHost, rs));
             }
             int status = 0;
-            SQ_CHECK(cudaMemcpyAsync(&status, status_.p, sizeof(int), cudaMemcpyDeviceToHost, rs));
+            if (r->dStatus)
+                SQ_CHECK(cudaMemcpyAsync(&status, r->dStatus, sizeof(int), cudaMemcpyDeviceToHost, rs));
             SQ_CHECK(cudaStreamSynchronize(rs));
+            r->status = status;
             cudaEventDestroy(r->done);
             r->done = nullptr;
             r->mem.release(st_.get());
@@ -516,7 +563,6 @@ private:
             completed_.push_back(r->id);
             ++done_;
             ++n;
-            throwErrorIf(status != 0, "a dense sweep kernel reported status %d.", status);
         }
         return n;
     }
@@ -552,7 +598,7 @@ private:
     std::deque<Request *> finishing_;  // last step queued, results not yet collected
     DevBuf<sq103_dense_task> dTasks_;
     DevBuf<sq103_bipartite_task> bTasks_;
-    DevBuf<int> dPos_, bPos_, counts_, queues_, status_;
+    DevBuf<int> dPos_, bPos_, counts_, queues_;
     DevBuf<float> dW_;
     static constexpr int kMaxPack = 8;  // instances per packed launch (sq103_dense_anneal_pack)
 };
@@ -623,6 +669,12 @@ SQ103_API int sq103_server_result(void *h, int id, double *E, int capE, int *m, 
         Server *s = as_server(h);
         const Server::Request &r = s->request(id);
         throwErrorIf(r.state != Server::kDone, "request %d is not done.", id);
+        if (r.status != 0) {
+            const int st = r.status;
+            if (release) s->release(id);
+            sqaod::throwError("request %d: its sweep gave up a bounded device wait (status %d); its spins and "
+                       "energies are not valid.", id, st);
+        }
         throwErrorIf((int)r.E.size() > capE, "energy capacity %d is smaller than %d.", capE, (int)r.E.size());
         if (E) memcpy(E, r.E.data(), sizeof(double) * r.E.size());
         if (m) *m = r.m;
@@ -631,6 +683,9 @@ SQ103_API int sq103_server_result(void *h, int id, double *E, int capE, int *m, 
         if (q1 && !r.q1.empty()) memcpy(q1, r.q1.data(), r.q1.size());
         if (release) s->release(id);
     });
+}
+SQ103_API int sq103_server_inject_status(void *h, int id, int value) {
+    return serve_guard([&] { as_server(h)->injectStatus(id, value); });
 }
 SQ103_API int sq103_server_set_large_limit(void *h, int n) {
     return serve_guard([&] { as_server(h)->setLargeLimit(n); });

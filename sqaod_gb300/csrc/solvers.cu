@@ -56,6 +56,23 @@ __global__ void sym_check_kernel(const float *W, int N, int ld, int *bad) {
     if (__syncthreads_or(mismatch) && tx == 0 && ty == 0) atomicOr(bad, 1);
 }
 
+// dst (rows x cols, row stride ldd) = fp32 rounding of src (row stride lds): the
+// fp32 copy of a <double> problem that the sweeps run on
+__global__ void round_to_f32(const double *src, int rows, int cols, int lds, float *dst, int ldd) {
+    const size_t n = (size_t)rows * cols;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = i / cols, c = i - r * cols;
+        dst[r * ldd + c] = (float)src[r * lds + c];
+    }
+}
+
+static void round_problem(const double *src, int rows, int cols, int lds, float *dst, int ldd, cudaStream_t st) {
+    const size_t n = (size_t)rows * cols;
+    const int grid = (int)std::min<size_t>((n + 255) / 256, 4096);
+    round_to_f32<<<grid, 256, 0, st>>>(src, rows, cols, lds, dst, ldd);
+    SQ_CHECK(cudaGetLastError());
+}
+
 // a matrix with row stride = columns
 template <class real>
 static std::vector<real> dense_copy(const sq::MatrixType<real> &M) {
@@ -127,6 +144,71 @@ public:
         setState(solRandSeedGiven);
     }
 
+    // <double> problems (sq::cuda::DenseGraphAnnealer<double>): the FP64 couplings
+    // are kept for the trials the fp32 sweep flags (their exact decisions) and for
+    // the energies; the sweep runs on their fp32 rounding.  W is N x N row-major.
+    void setQUBO64(const double *W, int N, sq::OptimizeMethod om) {
+        throwErrorIf(N <= 0, "%s, Shape does not match.", __func__);
+        throwErrorIf(!sq::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
+        clearState(solProblemSet);
+        N_ = N;
+        m_ = N_ / 4;
+        om_ = om;
+        allocProblem();
+        allocFP64();
+        const double sgn = om == sq::optMaximize ? -1. : 1.;  // maximize negates W (CUDADenseGraphAnnealer.cu:148-149)
+        std::vector<double> w((size_t)N * N);
+        for (size_t i = 0; i < w.size(); ++i) w[i] = sgn * W[i];
+        DevBuf<double> dW;
+        dW.ensure(w.size());
+        SQ_CHECK(cudaMemcpyAsync(dW.p, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(sq103_dense_hamiltonian64(dW.p, N_, d_h64_.p, d_J64_.p, d_c64_.p, d_scratchN_.p, st_.get()));
+        finishFP64();
+        setState(solProblemSet);
+    }
+
+    void setHamiltonian64(const double *h, const double *J, double c, int N) {
+        throwErrorIf(N <= 0, "%s, Shape does not match.", __func__);
+        throwErrorIf(!sq::isSymmetric(J, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
+        clearState(solProblemSet);
+        N_ = N;
+        m_ = N_ / 4;
+        om_ = sq::optMinimize;
+        allocProblem();
+        allocFP64();
+        SQ_CHECK(cudaMemcpyAsync(d_h64_.p, h, sizeof(double) * N_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_J64_.p, J, sizeof(double) * N_ * N_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
+        finishFP64();
+        setState(solProblemSet);
+    }
+
+    void getHamiltonian64(double *h, double *J, double *c) {
+        throwErrorIfProblemNotSet();
+        throwErrorIf(!fp64_, "%s, the problem is not a double-precision one.", __func__);
+        SQ_CHECK(cudaMemcpyAsync(h, d_h64_.p, sizeof(double) * N_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(J, d_J64_.p, sizeof(double) * N_ * N_, cudaMemcpyDeviceToHost, st_.get()));
+        *c = c64h_;
+        st_.sync();
+    }
+    bool isFP64() const { return fp64_; }
+
+    double getSystemE64(double G, double beta) {
+        calculate_E();
+        double E = 0.;
+        for (int y = 0; y < m_; ++y) E += h_E64_.p[y];
+        E /= m_;
+        if (sq::isSQAAlgorithm(algo_)) {
+            d_ring_.ensure(1);
+            SQ_CHECK(sq103_ring_dot(d_q_.p, N_, m_, d_ring_.p, st_.get()));
+            long long ring = 0;
+            SQ_CHECK(cudaMemcpyAsync(&ring, d_ring_.p, sizeof(ring), cudaMemcpyDeviceToHost, st_.get()));
+            st_.sync();
+            E -= (double)ring * 0.5 / beta * std::log(std::tanh(G * beta / (double)m_));
+        }
+        return om_ == sq::optMaximize ? -E : E;
+    }
+
     void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
         throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
         // the exact symmetry check (Common.cpp:97-104) runs on the uploaded copy,
@@ -143,7 +225,9 @@ public:
         allocProblem();
         SQ_CHECK(sq103_dense_hamiltonian(dW.p, N_, N_, om == sq::optMaximize, d_h_.p, d_J_.p, ldJ_, d_c_.p,
                                          d_c64_.p, d_scratchN_.p, st_.get()));
+        makeDigits();
         st_.sync();
+        dropFP64();
         setState(solProblemSet);
     }
 
@@ -170,10 +254,12 @@ public:
         allocProblem();
         SQ_CHECK(cudaMemcpyAsync(d_h_.p, h.data, sizeof(float) * N_, cudaMemcpyHostToDevice, st_.get()));
         upload(d_J_.p, ldJ_, J);
+        makeDigits();
         double c64 = (double)c;
         SQ_CHECK(cudaMemcpyAsync(d_c_.p, &c, sizeof(float), cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c64, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
         st_.sync();
+        dropFP64();
         setState(solProblemSet);
     }
 
@@ -198,6 +284,7 @@ public:
         size_t mn = (size_t)m_ * N_;
         d_q_.ensure(mn);
         d_F_.ensure(mn);
+        if (d_digits_.p) d_Abf_.ensure(sq103_tc_spins_bytes(m_, N_));
         d_E64_.ensure(m_);
         d_E32_.ensure(m_);
         h_E64_.ensure(m_);
@@ -250,8 +337,12 @@ public:
         throwErrorIfQNotSet();
         checkStatus();
         d_r_.ensure((size_t)m_ * N_);
-        SQ_CHECK(sq103_dense_energy(d_J_.p, ldJ_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize, d_r_.p,
-                                    d_E64_.p, d_E32_.p, st_.get()));
+        if (fp64_)
+            SQ_CHECK(sq103_dense_energy64(d_J64_.p, d_h64_.p, c64h_, d_q_.p, N_, m_, om_ == sq::optMaximize,
+                                          d_E64_.p, st_.get()));
+        else
+            SQ_CHECK(sq103_dense_energy(d_J_.p, ldJ_, d_h_.p, d_c64_.p, d_q_.p, N_, m_, om_ == sq::optMaximize,
+                                        d_r_.p, d_E64_.p, d_E32_.p, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(h_E64_.p, d_E64_.p, sizeof(double) * m_, cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
         E_.resize(m_);
@@ -368,6 +459,37 @@ private:
         d_c_.ensure(1);
         d_c64_.ensure(1);
         d_scratchN_.ensure(N_);
+        d_status_.ensure(1);
+        SQ_CHECK(cudaMemsetAsync(d_status_.p, 0, sizeof(int), st_.get()));
+        // large instances refresh their fields on the tensor cores from digit planes of J
+        if (sq103_dense_refresh_uses_tc(N_))
+            d_digits_.ensure(sq103_tc_digits_bytes(N_, N_));
+        else
+            d_digits_.release();
+    }
+
+    void makeDigits() {
+        if (d_digits_.p) SQ_CHECK(sq103_tc_make_digits(d_J_.p, ldJ_, N_, N_, 0, d_digits_.p, st_.get()));
+    }
+
+    void allocFP64() {
+        d_J64_.ensure((size_t)N_ * N_);
+        d_h64_.ensure(N_);
+    }
+    // the fp32 copies of an uploaded FP64 problem (h64, J64, c64), their digits, and c64 on the host
+    void finishFP64() {
+        round_problem(d_h64_.p, 1, N_, N_, d_h_.p, N_, st_.get());
+        round_problem(d_J64_.p, N_, N_, N_, d_J_.p, ldJ_, st_.get());
+        round_problem(d_c64_.p, 1, 1, 1, d_c_.p, 1, st_.get());
+        makeDigits();
+        SQ_CHECK(cudaMemcpyAsync(&c64h_, d_c64_.p, sizeof(double), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        fp64_ = true;
+    }
+    void dropFP64() {
+        fp64_ = false;
+        d_J64_.release();
+        d_h64_.release();
     }
 
     void upload(float *dst, int ldDst, const Matrix &M) {
@@ -384,7 +506,8 @@ private:
     }
 
     void refreshFields() {
-        SQ_CHECK(sq103_dense_field_refresh(d_J_.p, ldJ_, d_q_.p, d_F_.p, N_, m_, st_.get()));
+        SQ_CHECK(sq103_dense_refresh(d_J_.p, ldJ_, d_digits_.p, d_Abf_.p, d_q_.p, d_F_.p, N_, m_, d_status_.p,
+                                     st_.get()));
         stepsSinceRefresh_ = 0;
     }
 
@@ -431,6 +554,8 @@ private:
             t.nSteps = chunk;
             t.status = d_status_.p;
             t.flags = kernelFlags_;
+            t.J64 = fp64_ ? d_J64_.p : nullptr;
+            t.h64 = fp64_ ? d_h64_.p : nullptr;
             if (algo != kNaive) {
                 unsigned long long wsb = sq103_dense_ws_bytes(N_, m_, chunk);
                 d_ws_.ensure(wsb);
@@ -475,6 +600,10 @@ private:
 
     mutable Stream st_;
     DevBuf<float> d_J_, d_h_, d_c_, d_F_, d_E32_, d_sched_;
+    DevBuf<unsigned char> d_digits_, d_Abf_;  // tensor-core refresh: digit planes of J, spins in bf16
+    DevBuf<double> d_J64_, d_h64_;            // FP64 problem of a <double> annealer (J64 row stride N)
+    double c64h_ = 0.;
+    bool fp64_ = false;
     int ldJ_ = 0;  // row stride of J
     DevBuf<double> d_c64_, d_scratchN_, d_E64_, d_r_;
     DevBuf<int8_t> d_q_;
@@ -495,7 +624,10 @@ private:
 
 public:
     void setKernel(int flags) {
-        throwErrorIf(flags < 0 || flags > 2, "kernel selector must be 0 (auto), 1 (one CTA) or 2 (CTA per trotter).");
+        throwErrorIf(flags < 0 || (flags & kFlagKernelMask) > 2 ||
+                         (flags & ~(kFlagKernelMask | kFlagShortWaits | kFlagWithholdTrotter0)),
+                     "kernel selector must be 0 (auto), 1 (one CTA) or 2 (CTA per trotter), optionally with the "
+                     "test flags 16 (1 ms waits) and 32 (trotter 0 withholds its accept words).");
         kernelFlags_ = flags;
     }
 };
@@ -542,6 +674,77 @@ public:
         setState(solRandSeedGiven);
     }
 
+    // <double> problems: the FP64 couplings decide the flagged trials and give the
+    // energies; the sweeps run on their fp32 rounding.  W is N1 x N0 row-major.
+    void setQUBO64(const double *b0, const double *b1, const double *W, int N0, int N1, sq::OptimizeMethod om) {
+        throwErrorIf(N0 <= 0 || N1 <= 0, "%s, Shape does not match.", __func__);
+        clearState(solProblemSet);
+        N0_ = N0;
+        N1_ = N1;
+        m_ = (N0_ + N1_) / 4;
+        om_ = om;
+        allocProblem();
+        allocFP64();
+        const double sgn = om == sq::optMaximize ? -1. : 1.;
+        std::vector<double> v((size_t)N0 * N1 + N0 + N1);
+        for (size_t i = 0; i < (size_t)N0 * N1; ++i) v[i] = sgn * W[i];
+        for (int i = 0; i < N0; ++i) v[(size_t)N0 * N1 + i] = sgn * b0[i];
+        for (int i = 0; i < N1; ++i) v[(size_t)N0 * N1 + N0 + i] = sgn * b1[i];
+        DevBuf<double> dv, scr;
+        dv.ensure(v.size());
+        scr.ensure((size_t)N0 + 2 * N1);
+        SQ_CHECK(cudaMemcpyAsync(dv.p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(sq103_bipartite_hamiltonian64(dv.p + (size_t)N0 * N1, dv.p + (size_t)N0 * N1 + N0, dv.p, N0, N1,
+                                               d_h0_64_.p, d_h1_64_.p, d_J64_.p, d_c64_.p, scr.p, st_.get()));
+        finishFP64();
+        setState(solProblemSet);
+    }
+
+    void setHamiltonian64(const double *h0, const double *h1, const double *J, double c, int N0, int N1) {
+        throwErrorIf(N0 <= 0 || N1 <= 0, "%s, Shape does not match.", __func__);
+        clearState(solProblemSet);
+        N0_ = N0;
+        N1_ = N1;
+        m_ = (N0_ + N1_) / 4;
+        om_ = sq::optMinimize;
+        allocProblem();
+        allocFP64();
+        SQ_CHECK(cudaMemcpyAsync(d_h0_64_.p, h0, sizeof(double) * N0_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_h1_64_.p, h1, sizeof(double) * N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_J64_.p, J, sizeof(double) * N0_ * N1_, cudaMemcpyHostToDevice, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
+        finishFP64();
+        setState(solProblemSet);
+    }
+
+    void getHamiltonian64(double *h0, double *h1, double *J, double *c) {
+        throwErrorIfProblemNotSet();
+        throwErrorIf(!fp64_, "%s, the problem is not a double-precision one.", __func__);
+        SQ_CHECK(cudaMemcpyAsync(h0, d_h0_64_.p, sizeof(double) * N0_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(h1, d_h1_64_.p, sizeof(double) * N1_, cudaMemcpyDeviceToHost, st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(J, d_J64_.p, sizeof(double) * N0_ * N1_, cudaMemcpyDeviceToHost, st_.get()));
+        *c = c64h_;
+        st_.sync();
+    }
+    bool isFP64() const { return fp64_; }
+
+    double getSystemE64(double G, double beta) {
+        calculate_E();
+        double E = 0.;
+        for (int y = 0; y < m_; ++y) E += h_E64_.p[y];
+        E /= m_;
+        if (sq::isSQAAlgorithm(algo_)) {
+            d_ring_.ensure(2);
+            SQ_CHECK(sq103_ring_dot(d_q0_.p, N0_, m_, d_ring_.p, st_.get()));
+            SQ_CHECK(sq103_ring_dot(d_q1_.p, N1_, m_, d_ring_.p + 1, st_.get()));
+            long long ring[2] = {0, 0};
+            SQ_CHECK(cudaMemcpyAsync(ring, d_ring_.p, sizeof(ring), cudaMemcpyDeviceToHost, st_.get()));
+            st_.sync();
+            E -= (double)(ring[0] + ring[1]) * 0.5 / beta * std::log(std::tanh(G * beta / (double)m_));
+        }
+        return om_ == sq::optMaximize ? -E : E;
+    }
+
     void setQUBO(const Vector &b0, const Vector &b1, const Matrix &W, sq::OptimizeMethod om) override {
         throwErrorIf(W.cols != b0.size || W.rows != b1.size, "%s, Shape does not match.", __func__);
         clearState(solProblemSet);
@@ -560,7 +763,9 @@ public:
                                    cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(sq103_bipartite_hamiltonian(db0.p, db1.p, dW.p, N0_, N1_, om == sq::optMaximize, d_h0_.p, d_h1_.p,
                                              d_J_.p, d_c_.p, d_c64_.p, d_scratch_.p, st_.get()));
+        makeDigits();
         st_.sync();
+        dropFP64();
         setState(solProblemSet);
     }
 
@@ -579,7 +784,9 @@ public:
                                    N1_, cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(d_c_.p, &c, sizeof(float), cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(d_c64_.p, &c64, sizeof(double), cudaMemcpyHostToDevice, st_.get()));
+        makeDigits();
         st_.sync();
+        dropFP64();
         setState(solProblemSet);
     }
 
@@ -607,6 +814,7 @@ public:
         d_q1_.ensure((size_t)m_ * N1_);
         d_F0_.ensure((size_t)m_ * N0_);
         d_F1_.ensure((size_t)m_ * N1_);
+        if (d_digits1_.p) d_Abf_.ensure(sq103_tc_spins_bytes(m_, std::max(N0_, N1_)));
         d_E64_.ensure(m_);
         h_E64_.ensure(m_);
         h_q0_.ensure((size_t)m_ * N0_);
@@ -664,8 +872,12 @@ public:
     void calculate_E() override {
         throwErrorIfQNotSet();
         d_r_.ensure((size_t)m_ * N1_);
-        SQ_CHECK(sq103_bipartite_energy(d_J_.p, d_h0_.p, d_h1_.p, d_c64_.p, d_q0_.p, d_q1_.p, N0_, N1_, m_,
-                                        om_ == sq::optMaximize, d_r_.p, d_E64_.p, nullptr, st_.get()));
+        if (fp64_)
+            SQ_CHECK(sq103_bipartite_energy64(d_J64_.p, d_h0_64_.p, d_h1_64_.p, c64h_, d_q0_.p, d_q1_.p, N0_, N1_, m_,
+                                              om_ == sq::optMaximize, d_E64_.p, st_.get()));
+        else
+            SQ_CHECK(sq103_bipartite_energy(d_J_.p, d_h0_.p, d_h1_.p, d_c64_.p, d_q0_.p, d_q1_.p, N0_, N1_, m_,
+                                            om_ == sq::optMaximize, d_r_.p, d_E64_.p, nullptr, st_.get()));
         SQ_CHECK(cudaMemcpyAsync(h_E64_.p, d_E64_.p, sizeof(double) * m_, cudaMemcpyDeviceToHost, st_.get()));
         st_.sync();
         E_.resize(m_);
@@ -775,6 +987,45 @@ private:
         d_c_.ensure(1);
         d_c64_.ensure(1);
         d_scratch_.ensure(N0_ + N1_);
+        d_status_.ensure(1);
+        SQ_CHECK(cudaMemsetAsync(d_status_.p, 0, sizeof(int), st_.get()));
+        // large problems compute the half-step fields on the tensor cores from digit
+        // planes of J (for F1) and of J^T (for F0)
+        if (sq103_bipartite_refresh_uses_tc(N0_, N1_)) {
+            d_digits1_.ensure(sq103_tc_digits_bytes(N1_, N0_));
+            d_digits0_.ensure(sq103_tc_digits_bytes(N0_, N1_));
+        } else {
+            d_digits1_.release();
+            d_digits0_.release();
+        }
+    }
+
+    void makeDigits() {
+        if (!d_digits1_.p) return;
+        SQ_CHECK(sq103_tc_make_digits(d_J_.p, N0_, N1_, N0_, 0, d_digits1_.p, st_.get()));
+        SQ_CHECK(sq103_tc_make_digits(d_J_.p, N0_, N0_, N1_, 1, d_digits0_.p, st_.get()));
+    }
+
+    void allocFP64() {
+        d_J64_.ensure((size_t)N0_ * N1_);
+        d_h0_64_.ensure(N0_);
+        d_h1_64_.ensure(N1_);
+    }
+    void finishFP64() {
+        round_problem(d_h0_64_.p, 1, N0_, N0_, d_h0_.p, N0_, st_.get());
+        round_problem(d_h1_64_.p, 1, N1_, N1_, d_h1_.p, N1_, st_.get());
+        round_problem(d_J64_.p, N1_, N0_, N0_, d_J_.p, N0_, st_.get());
+        round_problem(d_c64_.p, 1, 1, 1, d_c_.p, 1, st_.get());
+        makeDigits();
+        SQ_CHECK(cudaMemcpyAsync(&c64h_, d_c64_.p, sizeof(double), cudaMemcpyDeviceToHost, st_.get()));
+        st_.sync();
+        fp64_ = true;
+    }
+    void dropFP64() {
+        fp64_ = false;
+        d_J64_.release();
+        d_h0_64_.release();
+        d_h1_64_.release();
     }
 
     void uploadQ() {
@@ -823,6 +1074,13 @@ private:
         t.m = m_;
         t.algo = algo;
         t.nSteps = nSteps;
+        t.J64 = fp64_ ? d_J64_.p : nullptr;
+        t.h0_64 = fp64_ ? d_h0_64_.p : nullptr;
+        t.h1_64 = fp64_ ? d_h1_64_.p : nullptr;
+        t.digits1 = d_digits1_.p;
+        t.digits0 = d_digits0_.p;
+        t.spinsBf16 = d_Abf_.p;
+        t.status = d_status_.p;
         SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
         step_ += (uint32_t)nSteps;
         clearState(solSolutionAvailable);
@@ -846,6 +1104,9 @@ private:
     mutable Stream st_;
     DevBuf<float> d_J_, d_h0_, d_h1_, d_c_, d_F0_, d_F1_, d_sched_;
     DevBuf<double> d_c64_, d_scratch_, d_E64_, d_r_;
+    DevBuf<double> d_J64_, d_h0_64_, d_h1_64_;        // FP64 problem of a <double> annealer
+    DevBuf<unsigned char> d_digits1_, d_digits0_, d_Abf_;  // tensor-core half-step fields
+    DevBuf<int> d_status_;
     DevBuf<int8_t> d_q0_, d_q1_;
     DevBuf<unsigned long long> d_acc_;
     DevBuf<long long> d_ring_;
@@ -856,7 +1117,138 @@ private:
     sq::BitSetPairArray xlist_, qlist_;
     unsigned long long seed_ = 0;
     uint32_t step_ = 0;
+    double c64h_ = 0.;
+    bool fp64_ = false;
     bool trace_ = false, accInit_ = false;
+};
+
+// ============================================== <double> annealers
+// sq::cuda::{Dense,Bipartite}GraphAnnealer<double> (the reference instantiates
+// both, CUDADenseGraphAnnealer.cu:607-608, CUDABipartiteGraphAnnealer.cu:647-648).
+// A float annealer carries the FP64 problem and does the work: its sweeps run on
+// the fp32 rounding of the couplings, every trial they flag is decided from the
+// FP64 couplings, and the energies are summed from them in FP64.  G and beta are
+// taken in fp32, the schedule's precision in every kernel.
+static sq::Preferences as_double_prefs(sq::Preferences prefs) {
+    for (int i = 0; i < (int)prefs.size(); ++i)
+        if (prefs[i].name == sq::pnPrecision) prefs[i] = sq::Preference(sq::pnPrecision, "double");
+    return prefs;
+}
+
+class DenseAnnealer64 : public sq::cuda::DenseGraphAnnealer<double> {
+public:
+    typedef sq::MatrixType<double> Matrix;
+    typedef sq::VectorType<double> Vector;
+
+    DenseAnnealer &inner() { return f_; }
+
+    void assignDevice(sq::cuda::Device &device) override { f_.assignDevice(device); }
+    sq::Algorithm selectAlgorithm(sq::Algorithm algo) override { return f_.selectAlgorithm(algo); }
+    sq::Algorithm getAlgorithm() const override { return f_.getAlgorithm(); }
+    sq::Preferences getPreferences() const override { return as_double_prefs(f_.getPreferences()); }
+    void setPreference(const sq::Preference &pref) override { f_.setPreference(pref); }
+    void seed(unsigned long long s) override { f_.seed(s); }
+
+    void setQUBO(const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.rows != W.cols, "%s, W is not a sqare matrix.", __func__);
+        std::vector<double> d = dense_copy(W);
+        f_.setQUBO64(d.data(), W.rows, om);
+        N_ = W.rows;
+    }
+    void setHamiltonian(const Vector &h, const Matrix &J, double c) override {
+        throwErrorIf(J.rows != J.cols, "%s, J is not a sqare matrix.", __func__);
+        throwErrorIf(h.size != J.cols, "%s, Shape does not match.", __func__);
+        std::vector<double> d = dense_copy(J);
+        f_.setHamiltonian64(h.data, d.data(), c, J.rows);
+        N_ = J.rows;
+    }
+    void getHamiltonian(Vector *h, Matrix *J, double *c) const override {
+        h->resize(N_);
+        J->resize(N_, N_);
+        std::vector<double> d((size_t)N_ * N_);
+        f_.getHamiltonian64(h->data, d.data(), c);
+        for (int i = 0; i < N_; ++i) memcpy(&(*J)(i, 0), d.data() + (size_t)i * N_, sizeof(double) * N_);
+    }
+    void prepare() override { f_.prepare(); }
+    void randomizeSpin() override { f_.randomizeSpin(); }
+    void set_q(const sq::BitSet &q) override { f_.set_q(q); }
+    void set_qset(const sq::BitSetArray &q) override { f_.set_qset(q); }
+    const sq::BitSetArray &get_q() const override { return f_.get_q(); }
+    const sq::BitSetArray &get_x() const override { return f_.get_x(); }
+    void annealOneStep(double G, double beta) override { f_.annealOneStep((float)G, (float)beta); }
+    void calculate_E() override { f_.calculate_E(); }
+    void makeSolution() override { f_.makeSolution(); }
+    double getSystemE(double G, double beta) const override { return f_.getSystemE64(G, beta); }
+    const Vector &get_E() const override {
+        std::vector<double> e;
+        f_.getE64(e);
+        E_.resize((sq::SizeType)e.size());
+        for (size_t i = 0; i < e.size(); ++i) E_((sq::IdxType)i) = e[i];
+        return E_;
+    }
+
+private:
+    mutable DenseAnnealer f_;
+    mutable Vector E_;
+};
+
+class BipartiteAnnealer64 : public sq::cuda::BipartiteGraphAnnealer<double> {
+public:
+    typedef sq::MatrixType<double> Matrix;
+    typedef sq::VectorType<double> Vector;
+
+    BipartiteAnnealer &inner() { return f_; }
+
+    void assignDevice(sq::cuda::Device &device) override { f_.assignDevice(device); }
+    sq::Algorithm selectAlgorithm(sq::Algorithm algo) override { return f_.selectAlgorithm(algo); }
+    sq::Algorithm getAlgorithm() const override { return f_.getAlgorithm(); }
+    sq::Preferences getPreferences() const override { return as_double_prefs(f_.getPreferences()); }
+    void setPreference(const sq::Preference &pref) override { f_.setPreference(pref); }
+    void seed(unsigned long long s) override { f_.seed(s); }
+
+    void setQUBO(const Vector &b0, const Vector &b1, const Matrix &W, sq::OptimizeMethod om) override {
+        throwErrorIf(W.cols != b0.size || W.rows != b1.size, "%s, Shape does not match.", __func__);
+        std::vector<double> d = dense_copy(W);
+        f_.setQUBO64(b0.data, b1.data, d.data(), b0.size, b1.size, om);
+        N0_ = b0.size;
+        N1_ = b1.size;
+    }
+    void setHamiltonian(const Vector &h0, const Vector &h1, const Matrix &J, double c) override {
+        throwErrorIf(J.cols != h0.size || J.rows != h1.size, "%s, Shape does not match.", __func__);
+        std::vector<double> d = dense_copy(J);
+        f_.setHamiltonian64(h0.data, h1.data, d.data(), c, h0.size, h1.size);
+        N0_ = h0.size;
+        N1_ = h1.size;
+    }
+    void getHamiltonian(Vector *h0, Vector *h1, Matrix *J, double *c) const override {
+        h0->resize(N0_);
+        h1->resize(N1_);
+        J->resize(N1_, N0_);
+        std::vector<double> d((size_t)N0_ * N1_);
+        f_.getHamiltonian64(h0->data, h1->data, d.data(), c);
+        for (int i = 0; i < N1_; ++i) memcpy(&(*J)(i, 0), d.data() + (size_t)i * N0_, sizeof(double) * N0_);
+    }
+    void prepare() override { f_.prepare(); }
+    void randomizeSpin() override { f_.randomizeSpin(); }
+    void set_q(const sq::BitSetPair &q) override { f_.set_q(q); }
+    void set_qset(const sq::BitSetPairArray &q) override { f_.set_qset(q); }
+    const sq::BitSetPairArray &get_q() const override { return f_.get_q(); }
+    const sq::BitSetPairArray &get_x() const override { return f_.get_x(); }
+    void annealOneStep(double G, double beta) override { f_.annealOneStep((float)G, (float)beta); }
+    void calculate_E() override { f_.calculate_E(); }
+    void makeSolution() override { f_.makeSolution(); }
+    double getSystemE(double G, double beta) const override { return f_.getSystemE64(G, beta); }
+    const Vector &get_E() const override {
+        std::vector<double> e;
+        f_.getE64(e);
+        E_.resize((sq::SizeType)e.size());
+        for (size_t i = 0; i < e.size(); ++i) E_((sq::IdxType)i) = e[i];
+        return E_;
+    }
+
+private:
+    mutable BipartiteAnnealer f_;
+    mutable Vector E_;
 };
 
 // ========================================================== BF searchers
@@ -893,6 +1285,25 @@ struct Pair {
     uint64_t x0, x1;
     bool operator<(const Pair &o) const { return x0 != o.x0 ? x0 < o.x0 : x1 < o.x1; }
 };
+
+// The <double> searchers screen every state with fp32 copies of the FP64
+// couplings: a value outside the fp32 range would become inf, and inf - inf
+// energies (NaN) fail every comparison, so true minimisers could be dropped
+// before the FP64 re-evaluation.  Such problems are refused, as is a total
+// magnitude at which some state's fp32 energy could overflow.
+static void checkScreeningRange(const double *a, size_t na, const double *b = nullptr, size_t nb = 0,
+                                const double *c = nullptr, size_t nc = 0) {
+    double total = 0.;
+    for (const auto &part : {std::make_pair(a, na), std::make_pair(b, nb), std::make_pair(c, nc)})
+        for (size_t i = 0; i < part.second; ++i) {
+            const double v = std::fabs(part.first[i]);
+            throwErrorIf(!(v <= (double)FLT_MAX), "setQUBO: a coupling of magnitude %g is not finite in float32, "
+                         "the precision of the screening pass.", part.first[i]);
+            total += v;
+        }
+    throwErrorIf(!(total <= 1e37), "setQUBO: the couplings' total magnitude %g could overflow the float32 "
+                 "energies of the screening pass.", total);
+}
 
 static float bf_slack(const std::vector<float> &vals) {
     bool integer = true;
@@ -946,6 +1357,7 @@ public:
         throwErrorIf(N <= 0, "%s, Shape does not match.", __func__);
         throwErrorIf(!sq::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
         throwErrorIf(63 < N, "N must be smaller than 64, N=%d.", N);
+        checkScreeningRange(W, (size_t)N * N);
         clearState(solProblemSet);
         N_ = N;
         om_ = om;
@@ -1143,6 +1555,7 @@ public:
         throwErrorIf(N0 <= 0 || N1 <= 0, "%s, Shape does not match.", __func__);
         throwErrorIf(63 < N0, "N0 must be smaller than 64, N0=%d.", N0);
         throwErrorIf(63 < N1, "N1 must be smaller than 64, N1=%d.", N1);
+        checkScreeningRange(b0, N0, b1, N1, W, (size_t)N0 * N1);
         clearState(solProblemSet);
         N0_ = N0;
         N1_ = N1;
@@ -1440,11 +1853,18 @@ public:
         bool multi = false;
         unsigned long long seed;
         DevBuf<unsigned char> mem, ws;
+        DevBuf<unsigned char> digits, Abf;  // tensor-core refresh (N >= 1024), as the single annealer
         unsigned long long wsBytes = 0;
         float *J, *h, *c32, *F;
         double *c64;
         int8_t *q;
+        int *status;
     };
+
+    void refresh(Inst &in) {
+        SQ_CHECK(sq103_dense_refresh(in.J, in.ldJ, in.digits.p, in.Abf.p, in.q, in.F, in.N, in.m, in.status,
+                                     st_.get()));
+    }
 
     ~DenseBatch() {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -1469,14 +1889,21 @@ public:
         in.h = (float *)(b + oh);
         in.c32 = (float *)(b + oc);
         in.c64 = (double *)(b + oc64);
+        in.status = (int *)(b + oc64 + 8);
         in.F = (float *)(b + oF);
         in.q = (int8_t *)(b + oq);
+        SQ_CHECK(cudaMemsetAsync(in.status, 0, sizeof(int), st_.get()));
+        if (sq103_dense_refresh_uses_tc(N)) {
+            in.digits.ensure(sq103_tc_digits_bytes(N, N));
+            in.Abf.ensure(sq103_tc_spins_bytes(m, N));
+        }
         dW_.ensure((size_t)N * N);
         scratch_.ensure(N);
         SQ_CHECK(cudaMemcpyAsync(dW_.p, W, sizeof(float) * N * N, cudaMemcpyHostToDevice, st_.get()));
         SQ_CHECK(cudaMemsetAsync(in.J, 0, sizeof(float) * N * in.ldJ, st_.get()));  // zero row padding
         SQ_CHECK(sq103_dense_hamiltonian(dW_.p, N, N, optimize, in.h, in.J, in.ldJ, in.c32, in.c64, scratch_.p,
                                          st_.get()));
+        if (in.digits.p) SQ_CHECK(sq103_tc_make_digits(in.J, in.ldJ, N, N, 0, in.digits.p, st_.get()));
         st_.sync();
         optimize_.push_back(optimize);
         return (int)insts_.size() - 1;
@@ -1504,7 +1931,7 @@ public:
         for (int i = 0; i < nAll; ++i) {
             Inst &in = *insts_[i];
             SQ_CHECK(sq103_randomize_spins(in.q, in.N, in.m, in.seed, 0, 0, st_.get()));
-            SQ_CHECK(sq103_dense_field_refresh(in.J, in.ldJ, in.q, in.F, in.N, in.m, st_.get()));
+            refresh(in);
             in.multi = multiMinN_ > 0 && in.N >= multiMinN_ && in.m >= 2 && sq103_dense_multicta_ok(in.N, in.m, kColoring);
             if (in.multi) {
                 in.wsBytes = sq103_dense_ws_bytes(in.N, in.m, kRefreshPeriod);
@@ -1740,7 +2167,7 @@ private:
     }
 
     void refreshAll() {
-        for (auto &p : insts_) SQ_CHECK(sq103_dense_field_refresh(p->J, p->ldJ, p->q, p->F, p->N, p->m, st_.get()));
+        for (auto &p : insts_) refresh(*p);
     }
 
     void captureStep() {
@@ -2188,6 +2615,14 @@ DenseGraphAnnealer<float> *newDenseGraphAnnealer<float>() {
 template <>
 BipartiteGraphAnnealer<float> *newBipartiteGraphAnnealer<float>() {
     return new sq103::BipartiteAnnealer();
+}
+template <>
+DenseGraphAnnealer<double> *newDenseGraphAnnealer<double>() {
+    return new sq103::DenseAnnealer64();
+}
+template <>
+BipartiteGraphAnnealer<double> *newBipartiteGraphAnnealer<double>() {
+    return new sq103::BipartiteAnnealer64();
 }
 template <>
 DenseGraphBFSearcher<float> *newDenseGraphBFSearcher<float>() {

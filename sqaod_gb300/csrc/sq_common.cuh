@@ -29,6 +29,15 @@ enum Tag : uint32_t {
 
 enum Algo : int { kNaive = 0, kColoring = 1, kSANaive = 2, kSAColoring = 3 };
 
+// sq103_dense_task.flags: bits 0-1 choose the kernel (0 auto, 1 one CTA per
+// instance, 2 one CTA per trotter); the other bits are test hooks of the
+// one-CTA-per-trotter sweep that make its bounded waits give up
+enum TaskFlags : int {
+    kFlagKernelMask = 3,
+    kFlagShortWaits = 16,        // every wait gives up after 1 ms instead of 4 s
+    kFlagWithholdTrotter0 = 32,  // trotter 0 never publishes its accept words
+};
+
 // device status words (written by kernels, read by the host)
 enum Status : int {
     kOk = 0,
@@ -128,6 +137,139 @@ __device__ __forceinline__ StepConst step_const(int algo, int m, float G, float 
         s.rate = beta;
     }
     return s;
+}
+
+// ------------------------------------------------------------ exact decisions
+// The resident fp32 fields drift from the exact local fields by the rounding
+// of their rank-1 updates (about 15 ulps after a few thousand updates).  Every
+// kernel takes its fp32 decision in the log form of the Metropolis test,
+//   accept iff dE < 0 or x = rate dE < L = -ln u,
+// and flags the trial when |x - L| lies within a bound on the fp32 error of x;
+// a flagged trial is decided again from its exact field, with the FP64
+// arithmetic of the host replay (exact_accept).  The sweeps thus take the FP64
+// decision on every trial whose FP64 acceptance margin is above about 1e-12,
+// and every kernel that runs the same trial takes the same decision.
+
+// -ln u of a uniform draw (+inf for u = 0: every finite x accepts, as exp(-x) > 0)
+__device__ __forceinline__ float neg_log_unit(float u) { return u > 0.f ? -logf(u) : __int_as_float(0x7f800000); }
+
+// The error bound of x = rate dE for a trial with field F: the field error is
+// taken as 2^-12 (|h| + |F| + 1) (dense fields enter dE as 2F, bipartite as F),
+// about 200 times the drift seen over the 8 steps between field refreshes; the
+// rest covers the rounding of the ring term, of x and of -ln u.
+struct DecisionTol {
+    float kF, kC;  // x tolerance = kF (|h| + |F'| + 1) + kC + 2.4e-7 L, F' = 2F (dense) or F
+};
+__device__ __forceinline__ DecisionTol decision_tol(bool sa, bool dense, float twoDivM, float coef, float rate) {
+    DecisionTol t;
+    const float dF = sa ? 2.f : twoDivM;  // d(dE) / d(h + F')
+    t.kF = __fmul_rn(__fmul_rn(rate, dF), 2.44140625e-4f);
+    t.kC = __fadd_rn(__fmul_rn(__fmul_rn(rate, 1e-6f), fabsf(coef)), 2e-6f);
+    (void)dense;
+    return t;
+}
+
+// accept iff dE < 0 or rate dE < L; nearFlag set when |rate dE - L| <= xtol
+__device__ __forceinline__ int metropolis_log(float dE, float rate, float L, float xtol, int &nearFlag) {
+    const float x = __fmul_rn(dE, rate);
+    if (fabsf(__fsub_rn(x, L)) <= xtol) nearFlag = 1;
+    return (dE < 0.f || x < L) ? 1 : 0;
+}
+
+// x tolerance of a trial: kF (|h| + |Fp| + 1) + kC + 2.4e-7 L (Fp = 2F dense, F bipartite)
+__device__ __forceinline__ float trial_xtol(const DecisionTol &t, float h, float Fp, float L) {
+    const float base = __fadd_rn(t.kC, __fmul_rn(2.4e-7f, fminf(L, 1e30f)));
+    return __fmaf_rn(t.kF, __fadd_rn(__fadd_rn(fabsf(h), fabsf(Fp)), 1.f), base);
+}
+
+// The exact local field sum_j J[j] q[j] (q = +-1) as an integer sum: every J[j]
+// is scaled by 2^S and rounded to an int64, S chosen from the row's largest
+// exponent and N so that no partial sum reaches 2^62.  Integer addition does not
+// depend on order, so a thread summing the row alone and a warp summing it in
+// 32 strands get the same value.  For fp32 couplings it is within N 2^-(S+1)
+// of the exact sum (4.5e-13 for |J| < 0.5 and N = 4096); the FP64 couplings of
+// the <double> annealers take the same scheme with the double exponent.
+template <class R>
+struct ExactFx;
+template <>
+struct ExactFx<float> {
+    static __device__ __forceinline__ unsigned expo(float v) { return (__float_as_uint(v) >> 23) & 0xffu; }
+    // |J| < 2^(E - 126) for biased exponent E
+    static __device__ __forceinline__ int shift(unsigned E, int lg) { return min(max(188 - lg - (int)E, -126), 127); }
+    static __device__ __forceinline__ long long term(float J, int S) {
+        return __float2ll_rn(__fmul_rn(J, __int_as_float((S + 127) << 23)));
+    }
+};
+template <>
+struct ExactFx<double> {
+    static __device__ __forceinline__ unsigned expo(double v) {
+        return (unsigned)((__double_as_longlong(v) >> 52) & 0x7ff);
+    }
+    // |J| < 2^(E - 1022) for biased exponent E
+    static __device__ __forceinline__ int shift(unsigned E, int lg) { return min(max(1084 - lg - (int)E, -1000), 1000); }
+    static __device__ __forceinline__ long long term(double J, int S) {
+        return __double2ll_rn(__dmul_rn(J, __longlong_as_double((long long)(1023 + S) << 52)));
+    }
+};
+__device__ __forceinline__ int log2_ceil(int N) { return N > 1 ? 32 - __clz(N - 1) : 0; }
+__device__ __forceinline__ double exact_value(long long s, int S) {
+    return __dmul_rn(__ll2double_rn(s), __longlong_as_double((long long)(1023 - S) << 52));
+}
+
+// one thread; the couplings are Jx[j * stride] (a row of J, or a column with stride = ld)
+template <class R>
+static __device__ __noinline__ double exact_field_thread(const R *Jx, size_t stride, const int8_t *q, int N) {
+    unsigned e = 0;
+    for (int j = 0; j < N; ++j) e = max(e, ExactFx<R>::expo(Jx[j * stride]));
+    const int S = ExactFx<R>::shift(e, log2_ceil(N));
+    long long s = 0;
+    for (int j = 0; j < N; ++j) {
+        const long long v = ExactFx<R>::term(Jx[j * stride], S);
+        s += q[j] > 0 ? v : -v;
+    }
+    return exact_value(s, S);
+}
+
+// warp-wide: every lane of the (converged) warp calls it and gets the sum
+template <class R>
+static __device__ __noinline__ double exact_field_warp(const R *Jx, const int8_t *q, int N) {
+    const int lane = threadIdx.x & 31;
+    unsigned e = 0;
+    for (int j = lane; j < N; j += 32) e = max(e, ExactFx<R>::expo(Jx[j]));
+    e = __reduce_max_sync(0xffffffffu, e);
+    const int S = ExactFx<R>::shift(e, log2_ceil(N));
+    long long s = 0;
+    for (int j = lane; j < N; j += 32) {
+        const long long v = ExactFx<R>::term(Jx[j], S);
+        s += q[j] > 0 ? v : -v;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return exact_value(s, S);
+}
+
+// FP64 decision of a dense trial from its exact field F, in the host replay's
+// order of operations: SQA dE = (2/m) q (h + 2F) - q (qL + qR) coef with
+// coef = log(tanh(G beta / m)) / beta, rate beta; SA dE = 2 q (h + 2F), rate 1/G;
+// accept iff dE < 0 or exp(-dE rate) > u.  For bipartite trials (dE with h + F)
+// pass twoF = false.
+static __device__ __noinline__ int exact_accept(bool sa, bool twoF, float q, double h, double F, float qL, float qR,
+                                                int m, float G, float beta, float u) {
+    const double qd = q, hd = h, Gd = G, bd = beta;
+    const double t = __dadd_rn(hd, twoF ? __dmul_rn(2.0, F) : F);
+    double dE, rate;
+    if (sa) {
+        dE = __dmul_rn(__dmul_rn(2.0, qd), t);
+        rate = 1.0 / Gd;
+    } else {
+        const double coef = log(tanh(__dmul_rn(Gd, bd) / (double)m)) / bd;
+        const double a = __dmul_rn(__dmul_rn(2.0 / (double)m, qd), t);
+        const double b = __dmul_rn(__dmul_rn(qd, (double)((int)qL + (int)qR)), coef);
+        dE = __dsub_rn(a, b);
+        rate = bd;
+    }
+    if (dE < 0.0) return 1;
+    return exp(__dmul_rn(-dE, rate)) > (double)u ? 1 : 0;
 }
 #endif
 

@@ -6,8 +6,12 @@ dense_graph_bf_searcher,bipartite_graph_bf_searcher}.py over the base
 classes of sqaodpy/sqaod/common/*_base.py.  Every method forwards to one
 handle-layer entry point of the C ABI (include/sqaod_gb300.h).
 
-The annealers take dtype numpy.float32; the brute-force searchers float32 or
-float64 (the <double> searchers, exact FP64 minima); other dtypes raise.
+Every solver takes dtype numpy.float32 or numpy.float64 (the reference's
+<double> instantiations: FP64 couplings, FP64 energies and minima; the
+annealers' sweeps run on the fp32 rounding of the couplings and decide every
+flagged trial from the FP64 ones); other dtypes raise.  The factories here
+default to float32; the reference's default to float64 and pass the dtype on,
+so code written against the reference gets the <double> solvers.
 """
 import ctypes
 
@@ -21,12 +25,10 @@ _c_float = ctypes.c_float
 
 
 def _check_dtype(dtype):
-    if dtype is None:
-        return np.float32
-    if np.dtype(dtype) != np.float32:
-        raise RuntimeError("dtype %s is not provided: the solvers compute in float32 only "
-                           "(the formulas also in float64)." % np.dtype(dtype))
-    return np.float32
+    d = np.dtype(np.float32 if dtype is None else dtype)
+    if d not in (np.float32, np.float64):
+        raise RuntimeError("dtype %s is not provided: the solvers compute in float32 or float64." % d)
+    return d.type
 
 
 def _pref_value(v):
@@ -102,7 +104,8 @@ class DenseGraphAnnealer(_Handle):
 
     def __init__(self, W, optimize, dtype, prefdict):
         self.dtype = _check_dtype(dtype)
-        super().__init__()
+        self._f64 = self.dtype is np.float64
+        super().__init__('sq103_dg_annealer64_new' if self._f64 else None)
         self._optimize = common.minimize
         if W is not None:
             self.set_qubo(W, optimize)
@@ -115,14 +118,18 @@ class DenseGraphAnnealer(_Handle):
         common.check_square(W)
         W = common.fix_type(W, self.dtype)
         om = _c_int(common.optimize_flag(optimize))
-        common.submit_symmetric(W, self.dtype, lambda w: self._call('set_qubo', ptr(w), _c_int(w.shape[0]), om))
+        fn = 'set_qubo64' if self._f64 else 'set_qubo'
+        common.submit_symmetric(W, self.dtype, lambda w: self._call(fn, ptr(w), _c_int(w.shape[0]), om))
         self._optimize = optimize
 
     def set_hamiltonian(self, h, J, c):
         common.check_square(J, 'J')
         h, J = common.fix_type([np.asarray(h), np.asarray(J)], self.dtype)
         J = np.ascontiguousarray(common.symmetrize(J), self.dtype)
-        self._call('set_hamiltonian', ptr(h), ptr(J), _c_float(float(c)), _c_int(J.shape[0]))
+        if self._f64:
+            self._call('set_hamiltonian64', ptr(h), ptr(J), ctypes.c_double(float(c)), _c_int(J.shape[0]))
+        else:
+            self._call('set_hamiltonian', ptr(h), ptr(J), _c_float(float(c)), _c_int(J.shape[0]))
         self._optimize = common.minimize
 
     def get_problem_size(self):
@@ -134,6 +141,8 @@ class DenseGraphAnnealer(_Handle):
         return self.get_preferences()['n_trotters']
 
     def get_E(self):
+        if self._f64:
+            return self.get_E64()
         cap = max(self._m(), 1)
         E = np.zeros(cap, np.float32)
         n = _c_int()
@@ -177,7 +186,7 @@ class DenseGraphAnnealer(_Handle):
         h = np.empty(N, self.dtype)
         J = np.empty((N, N), self.dtype)
         c = np.empty(1, self.dtype)
-        self._call('get_hamiltonian', ptr(h), ptr(J), ptr(c))
+        self._call('get_hamiltonian64' if self._f64 else 'get_hamiltonian', ptr(h), ptr(J), ptr(c))
         return h, J, c[0]
 
     def randomize_spin(self):
@@ -194,6 +203,10 @@ class DenseGraphAnnealer(_Handle):
         self._call('make_solution')
 
     def get_system_E(self, G, beta):
+        if self._f64:
+            E = ctypes.c_double()
+            self._call('get_system_E64', ctypes.c_double(G), ctypes.c_double(beta), ctypes.byref(E))
+            return np.float64(E.value)
         E = _c_float()
         self._call('get_system_E', _c_float(G), _c_float(beta), ctypes.byref(E))
         return np.float32(E.value)
@@ -261,7 +274,8 @@ class BipartiteGraphAnnealer(_Handle):
 
     def __init__(self, b0, b1, W, optimize, dtype, prefdict):
         self.dtype = _check_dtype(dtype)
-        super().__init__()
+        self._f64 = self.dtype is np.float64
+        super().__init__('sq103_bg_annealer64_new' if self._f64 else None)
         self._optimize = common.minimize
         if W is not None:
             self.set_qubo(b0, b1, W, optimize)
@@ -274,16 +288,20 @@ class BipartiteGraphAnnealer(_Handle):
         b0, b1, W = common.fix_type([np.asarray(b0), np.asarray(b1), np.asarray(W)], self.dtype)
         if W.ndim != 2 or W.shape != (len(b1), len(b0)):
             raise RuntimeError('dimension mismatch for b0, b1, W.')
-        self._call('set_qubo', ptr(b0), ptr(b1), ptr(W), _c_int(len(b0)), _c_int(len(b1)),
-                   _c_int(common.optimize_flag(optimize)))
+        self._call('set_qubo64' if self._f64 else 'set_qubo', ptr(b0), ptr(b1), ptr(W), _c_int(len(b0)),
+                   _c_int(len(b1)), _c_int(common.optimize_flag(optimize)))
         self._optimize = optimize
 
     def set_hamiltonian(self, h0, h1, J, c):
         h0, h1, J = common.fix_type([np.asarray(h0), np.asarray(h1), np.asarray(J)], self.dtype)
         if J.ndim != 2 or J.shape != (len(h1), len(h0)):
             raise RuntimeError('dimension mismatch for h0, h1, J.')
-        self._call('set_hamiltonian', ptr(h0), ptr(h1), ptr(J), _c_float(float(c)), _c_int(len(h0)),
-                   _c_int(len(h1)))
+        if self._f64:
+            self._call('set_hamiltonian64', ptr(h0), ptr(h1), ptr(J), ctypes.c_double(float(c)), _c_int(len(h0)),
+                       _c_int(len(h1)))
+        else:
+            self._call('set_hamiltonian', ptr(h0), ptr(h1), ptr(J), _c_float(float(c)), _c_int(len(h0)),
+                       _c_int(len(h1)))
         self._optimize = common.minimize
 
     def get_problem_size(self):
@@ -295,6 +313,8 @@ class BipartiteGraphAnnealer(_Handle):
         return self.get_preferences()['n_trotters']
 
     def get_E(self):
+        if self._f64:
+            return self.get_E64()
         cap = max(self._m(), 1)
         E = np.zeros(cap, np.float32)
         n = _c_int()
@@ -340,7 +360,7 @@ class BipartiteGraphAnnealer(_Handle):
         h1 = np.empty(N1, self.dtype)
         J = np.empty((N1, N0), self.dtype)
         c = np.empty(1, self.dtype)
-        self._call('get_hamiltonian', ptr(h0), ptr(h1), ptr(J), ptr(c))
+        self._call('get_hamiltonian64' if self._f64 else 'get_hamiltonian', ptr(h0), ptr(h1), ptr(J), ptr(c))
         return h0, h1, J, c[0]
 
     def randomize_spin(self):
@@ -356,6 +376,10 @@ class BipartiteGraphAnnealer(_Handle):
         self._call('make_solution')
 
     def get_system_E(self, G, beta):
+        if self._f64:
+            E = ctypes.c_double()
+            self._call('get_system_E64', ctypes.c_double(G), ctypes.c_double(beta), ctypes.byref(E))
+            return np.float64(E.value)
         E = _c_float()
         self._call('get_system_E', _c_float(G), _c_float(beta), ctypes.byref(E))
         return np.float32(E.value)
@@ -464,10 +488,15 @@ class DenseGraphBFSearcher(_Handle):
         self._call('make_solution')
 
     def search_range(self):
+        return self.search_range_state()[0]
+
+    def search_range_state(self):
+        """One searchRange step: (done, x) with x the next packed state to search
+        (the reference extension's return value, sqaodc/pyglue/bf_searcher.inc:408-424)."""
         x = ctypes.c_ulonglong()
         done = _c_int()
         self._call('search_range', ctypes.byref(x), ctypes.byref(done))
-        return bool(done.value)
+        return bool(done.value), x.value
 
     def search(self):
         self._call('search')
@@ -541,10 +570,15 @@ class BipartiteGraphBFSearcher(_Handle):
         self._call('make_solution')
 
     def search_range(self):
+        return self.search_range_state()[0]
+
+    def search_range_state(self):
+        """One searchRange step: (done, x0, x1), the next packed states to search
+        (sqaodc/pyglue/bf_searcher.inc:432-448)."""
         x0, x1 = ctypes.c_ulonglong(), ctypes.c_ulonglong()
         done = _c_int()
         self._call('search_range', ctypes.byref(x0), ctypes.byref(x1), ctypes.byref(done))
-        return bool(done.value)
+        return bool(done.value), x0.value, x1.value
 
     def search(self):
         self._call('search')

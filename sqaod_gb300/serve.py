@@ -90,6 +90,19 @@ class AnnealServer:
         self._call("state", ctypes.c_int(rid), ctypes.byref(s))
         return s.value
 
+    def state_or_none(self, rid):
+        """The request's state, or None once it has been released."""
+        s = ctypes.c_int()
+        if self._L.sq103_server_state(self._h, ctypes.c_int(rid), ctypes.byref(s)) != 0:
+            return None
+        return s.value
+
+    def inject_status(self, rid, value=1):
+        """Fault injection for tests: marks an active dense request as if its
+        sweep had given up a bounded device wait.  Its result() then raises;
+        every other request is unaffected."""
+        self._call("inject_status", ctypes.c_int(rid), ctypes.c_int(int(value)))
+
     def stats(self):
         v = [ctypes.c_int() for _ in range(3)]
         b = ctypes.c_ulonglong()
@@ -117,10 +130,13 @@ class AnnealServer:
         q1 = np.zeros((m, max(N1, 1)), np.int8)
         mm = ctypes.c_int()
         cap = max(q0.nbytes, q1.nbytes)
-        self._call("result", ctypes.c_int(rid), ptr(E), ctypes.c_int(m), ctypes.byref(mm), ptr(q0), ptr(q1),
-                   ctypes.c_longlong(cap), ctypes.c_int(1 if release else 0))
-        if release:
-            del self._shape[rid]
+        try:
+            self._call("result", ctypes.c_int(rid), ptr(E), ctypes.c_int(m), ctypes.byref(mm), ptr(q0), ptr(q1),
+                       ctypes.c_longlong(cap), ctypes.c_int(1 if release else 0))
+        finally:
+            # a request whose sweep gave up a device wait raises here, and is released all the same
+            if release and self.state_or_none(rid) is None:
+                self._shape.pop(rid, None)
         if N1 == 0:
             return E, q0
         return E, (q0, q1[:, :N1])

@@ -3,10 +3,11 @@
 The reference package ``sqaod`` refuses to import without its C extensions,
 so this script registers a bare package object for ``sqaod`` that points at the
 reference's ``sqaodpy/sqaod`` directory and imports only the pure-numpy
-modules (``sqaod.common`` and ``sqaod.py``).  Run it in a checkout that has the
-reference tree (default /root/reference, or $SQAOD_REFERENCE_ROOT):
+modules (``sqaod.common`` and ``sqaod.py``).  The reference tree is the first
+argument, else $SQAOD_REFERENCE_ROOT, else a directory named ``reference``
+beside this repository's root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [path/to/sqaod]
 
 The output is small (a few hundred KB) and is committed, so that the tests
 need no reference tree at run time.
@@ -29,7 +30,9 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("SQAOD_REFERENCE_ROOT", "/root/reference")
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+REF = (sys.argv[1] if len(sys.argv) > 1 else
+       os.environ.get("SQAOD_REFERENCE_ROOT", os.path.join(os.path.dirname(REPO), "reference")))
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
 
 

@@ -104,8 +104,9 @@ def test_state_machine_errors_on_host():
 
 def test_input_checks_on_host():
     import sqaod_gb300 as sq
-    with pytest.raises(RuntimeError):
-        sq.cuda.dense_graph_annealer(dtype=np.float64)
+    for make in (sq.cuda.dense_graph_annealer, sq.cuda.bipartite_graph_annealer, sq.cuda.dense_graph_bf_searcher):
+        with pytest.raises(RuntimeError, match="float32 or float64"):
+            make(dtype=np.int32)
     a = sq.cuda.dense_graph_annealer()
     W = np.random.default_rng(0).uniform(-1, 1, (6, 6)).astype(np.float32)
     with pytest.raises(RuntimeError):  # neither symmetric nor triangular

@@ -46,6 +46,8 @@ def test_searcher_dtypes():
                  lambda d: sq.cuda.bipartite_graph_bf_searcher(dtype=d)):
         with pytest.raises(RuntimeError, match="float32 or float64"):
             make(np.float16)
-    # the annealers are float32 only
-    with pytest.raises(RuntimeError, match="float32 only"):
-        sq.cuda.dense_graph_annealer(dtype=np.float64)
+    # so do the annealers (the <double> annealers keep FP64 couplings); other dtypes raise
+    for make in (lambda d: sq.cuda.dense_graph_annealer(dtype=d),
+                 lambda d: sq.cuda.bipartite_graph_annealer(dtype=d)):
+        with pytest.raises(RuntimeError, match="float32 or float64"):
+            make(np.float16)

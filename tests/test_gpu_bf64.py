@@ -92,3 +92,18 @@ def test_bipartite_bf64_matches_fp64_exhaustive():
     best, ref = _argmin_set(orc.bg_energy_qubo(b0, b1, W, x0, x1), 1., lambda i: (tuple(x0[i]), tuple(x1[i])))
     assert abs(E[0] - best) <= 1e-12 * max(1., abs(best))
     assert {(tuple(a), tuple(b)) for a, b in xs} == ref
+
+
+@pytest.mark.parametrize("bad", [1e39, float("inf")])
+def test_bf64_rejects_couplings_beyond_float32(bad):
+    """The fp32 screening pass cannot represent such couplings (inf - inf energies
+    would drop true minimisers), so the <double> searchers refuse the problem."""
+    import sqaod_gb300 as sq
+    W = np.zeros((8, 8))
+    W[2, 3] = W[3, 2] = bad
+    with pytest.raises(RuntimeError, match="float32"):
+        sq.cuda.dense_graph_bf_searcher(W, sq.minimize, dtype=F64)
+    b0, b1, Wb = np.zeros(4), np.zeros(5), np.zeros((5, 4))
+    Wb[1, 1] = bad
+    with pytest.raises(RuntimeError, match="float32"):
+        sq.cuda.bipartite_graph_bf_searcher(b0, b1, Wb, sq.minimize, dtype=F64)

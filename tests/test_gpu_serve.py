@@ -63,9 +63,9 @@ def test_server_requests_match_alone():
             N0, N1 = sizes
             data.append((rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32),
                          rng.uniform(-1, 1, (N1, N0)).astype(np.float32)))
-    # the N=1024 request (about 5 MB) waits until enough of the others finish; one
+    # the N=1024 request (about 14 MB with its digit planes) waits until enough of the others finish; one
     # large instance at a time
-    srv = AnnealServer(budget_bytes=6 << 20, max_slots=3)
+    srv = AnnealServer(budget_bytes=16 << 20, max_slots=3)
     srv.set_large_limit(1)
     ids = []
     for i, (spec, d) in enumerate(zip(SPECS, data)):
@@ -128,3 +128,79 @@ def test_server_rejects_oversized_request():
     with pytest.raises(SqaodError, match="exceeds the device-memory budget"):
         srv.submit_dense(_sym(np.random.default_rng(0), 1024), 4, G, beta, sq.minimize)
     assert srv.stats()["queued"] == 0
+
+
+def test_server_admits_arrivals_between_ticks():
+    """Requests submitted while others are on the GPU (between tick() calls,
+    under a budget and slot limit that make some wait) start as memory and slots
+    free up; each ends bit-identical to annealing it alone."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    rng = np.random.default_rng(31)
+    waves = [[("d", 300, 16, 20, "min"), ("b", (64, 80), 8, 14, "min")],
+             [("d", 1024, 32, 17, "min"), ("d", 50, 1, 9, "max")],
+             [("b", (40, 24), 1, 12, "min"), ("d", 180, 8, 30, "min"), ("d", 700, 16, 10, "min")]]
+    srv = AnnealServer(budget_bytes=16 << 20, max_slots=2)
+    srv.set_large_limit(1)
+    subs = []
+    for w, wave in enumerate(waves):
+        for spec in wave:
+            kind, sizes, m, steps, opt = spec
+            G, beta = _schedule(steps)
+            o = sq.maximize if opt == "max" else sq.minimize
+            seed = 3000 + len(subs)
+            if kind == "d":
+                d = _sym(rng, sizes)
+                rid = srv.submit_dense(d, m, G, beta, o, seed=seed)
+            else:
+                N0, N1 = sizes
+                d = (rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32),
+                     rng.uniform(-1, 1, (N1, N0)).astype(np.float32))
+                rid = srv.submit_bipartite(d[0], d[1], d[2], m, G, beta, o, seed=seed)
+            subs.append((spec, d, seed, rid))
+        if w < len(waves) - 1:
+            srv.tick()
+            s = srv.stats()
+            assert s["active"] > 0  # the next wave arrives while these are on the GPU
+    assert srv.run(max_ticks=200) < 200
+    for spec, d, seed, rid in subs:
+        E, q = srv.result(rid)
+        E1, q1 = _alone(sq, spec, d, seed)
+        assert np.array_equal(E, E1), (spec, E, E1)
+        if spec[0] == "d":
+            assert np.array_equal(q, np.array(q1)), spec
+        else:
+            assert np.array_equal(q[0], np.array([p[0] for p in q1])), spec
+            assert np.array_equal(q[1], np.array([p[1] for p in q1])), spec
+
+
+def test_server_status_is_per_request():
+    """A dense request whose status word reports a given-up device wait (set
+    from the host, as the sweep would) fails alone: the others, and requests
+    submitted after it, still complete and match their single-instance runs."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    rng = np.random.default_rng(41)
+    specs = [("d", 64, 4, 16, "min"), ("d", 1024, 16, 16, "min"), ("d", 96, 8, 16, "min")]
+    data = [_sym(rng, sp[1]) for sp in specs]
+    srv = AnnealServer(budget_bytes=1 << 30)
+    ids = []
+    for i, (spec, d) in enumerate(zip(specs, data)):
+        G, beta = _schedule(spec[3])
+        ids.append(srv.submit_dense(d, spec[2], G, beta, sq.minimize, seed=4000 + i))
+    srv.tick()
+    srv.inject_status(ids[1], 1)  # the large (one-CTA-per-trotter) request
+    assert srv.run(max_ticks=50) < 50
+    with pytest.raises(RuntimeError, match="bounded device wait"):
+        srv.result(ids[1])
+    assert srv.state_or_none(ids[1]) is None  # released all the same
+    for i in (0, 2):
+        E, q = srv.result(ids[i])
+        E1, q1 = _alone(sq, specs[i], data[i], 4000 + i)
+        assert np.array_equal(E, E1) and np.array_equal(q, np.array(q1))
+    G, beta = _schedule(16)
+    late = srv.submit_dense(data[1], 16, G, beta, sq.minimize, seed=4001)
+    assert srv.run(max_ticks=50) < 50
+    E, q = srv.result(late)
+    E1, q1 = _alone(sq, specs[1], data[1], 4001)
+    assert np.array_equal(E, E1) and np.array_equal(q, np.array(q1))

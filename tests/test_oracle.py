@@ -185,3 +185,57 @@ def test_replay_self_consistency(orc):
     trace = np.full((N * m + 31) // 32, 0xffffffff, np.uint32)
     q2, st = orc.dg_replay(h, J, m, orc.ALGO_COLORING, 7, 1, 1.0, 10.0, q, trace)
     assert st["n_trials"] == N * m and st["n_accept"] == N * m
+
+
+@pytest.mark.parametrize("algo", ["ALGO_COLORING", "ALGO_NAIVE", "ALGO_SA_NAIVE"])
+@pytest.mark.parametrize("N,m", [(40, 6), (33, 7)])
+def test_replay_steps_equals_per_step_replay(orc, algo, N, m):
+    """The resident-FP64-field replay (used at the benchmark size) takes the same
+    decisions and reports the same statistics as the direct-dot replay, over
+    several steps of a random device trace (about 6 % accepts)."""
+    rng = np.random.default_rng(N * m)
+    W = rng.uniform(-1, 1, (N, N))
+    W = np.triu(W) + np.triu(W, 1).T
+    h, J, c = orc.dg_hamiltonian(W)
+    h, J = h.astype(np.float32), J.astype(np.float32)
+    assert np.array_equal(J, J.T) and not np.diag(J).any()
+    q0 = orc.gpu_randomize(11, 0, 0, m, N)
+    G = np.array([3.0, 1.0, 0.3, 0.05], np.float32)
+    beta = np.array([10.0, 20.0, 30.0, 50.0], np.float32)
+    words = (N * m + 31) // 32
+    bits = rng.random((len(G), words * 32)) < 0.06
+    trace = np.packbits(bits, axis=1, bitorder="little").view(np.uint32)
+    a = getattr(orc, algo)
+    q, tot = q0.copy(), {}
+    for s in range(len(G)):
+        q, st = orc.dg_replay(h, J, m, a, 11, 5 + s, float(G[s]), float(beta[s]), q, trace[s])
+        for k, v in st.items():
+            tot[k] = max(tot.get(k, 0), v) if k == "max_mismatch_margin" else tot.get(k, 0) + v
+    q2, st2 = orc.dg_replay_steps(h, J, m, a, 11, 5, G, beta, q0, trace)
+    assert np.array_equal(q, q2)
+    assert tot["n_trials"] == st2["n_trials"] == len(G) * N * m
+    for k in ("n_accept", "n_mismatch", "n_mismatch_small", "n_small_margin"):
+        assert tot[k] == st2[k], (k, tot, st2)
+    assert tot["n_mismatch"] > 0  # a random trace disagrees with FP64 somewhere
+
+
+@pytest.mark.parametrize("N,om,lo,hi", [(16, 0, -8, 9), (20, 1, -8, 9), (18, 0, -1, 2), (13, 1, 0, 2)])
+def test_exact_int_search_equals_reference_searcher(orc, N, om, lo, hi):
+    """The Gray-code integer search (the checker at N = 32) gives the restated
+    reference CPU searcher's minimum and minimiser list, ties and the
+    tileSize cap included (the narrow ranges make many minimisers)."""
+    rng = np.random.default_rng(N + om)
+    U = np.triu(rng.integers(lo, hi, (N, N)))
+    W = (U + np.triu(U, 1).T).astype(np.float32)
+    for tile in (1024, 16):
+        E_ref, xs_ref = orc.dg_bf_search_ref(W, om, tile_size=tile)
+        E, xs, count = orc.dg_bf_search_exact_int(W, om, cap=tile)
+        assert E == E_ref and xs.tolist() == xs_ref.tolist(), (E, E_ref, count)
+        assert count >= len(xs)
+    assert orc.dg_bf_search_exact_int(W, om, cap=1 << 16)[2] == count
+
+
+def test_exact_int_search_rejects_non_integer(orc):
+    W = np.full((8, 8), 0.5, np.float32)
+    with pytest.raises(ValueError):
+        orc.dg_bf_search_exact_int(W)
