@@ -434,6 +434,9 @@ SQ103_API int sq103_dg_bf_search(void *handle);
  * minimum found so far (signed for the optimisation direction). */
 SQ103_API int sq103_dg_bf_search_subrange(void *handle, unsigned long long xBegin, unsigned long long xEnd);
 SQ103_API int sq103_dg_bf_get_E64(void *handle, double *E);
+/* No counterpart in the reference: the number of rows sq103_dg_bf_get_x
+ * returns (the minimisers kept, at most tile_size), to size its buffer. */
+SQ103_API int sq103_dg_bf_solution_count(void *handle, int *n);
 
 SQ103_API int sq103_bg_bf_new(void **handle);
 /* The <double> bipartite searcher, as sq103_dg_bf64_new above (W: N1 x N0). */
@@ -548,7 +551,7 @@ SQ103_API int sq103_bg_formulas64_calculate_E_from_spin(void *handle, const doub
                                                         const int8_t *q0, const int8_t *q1, int m, double *E);
 
 /* ------------------------------------------- handle layer: request server */
-/* Continuous batching of anneal requests of mixed size and type (no
+/* Continuous batching of anneal and search requests of mixed size and type (no
  * counterpart in the reference).  Requests are admitted in arrival order while
  * their device-memory footprint fits budgetBytes and a slot is free (one that
  * cannot start yet does not block the ones behind it); every
@@ -568,6 +571,18 @@ SQ103_API int sq103_server_submit_bipartite(void *handle, const float *b0, const
                                             const float *G, const float *beta, int nSteps, int *id);
 SQ103_API int sq103_server_tick(void *handle, int *completed);
 SQ103_API int sq103_server_state(void *handle, int id, int *state);
+/* A dense brute-force search request (W symmetric N x N, N < 64; the
+ * reference's unit of work is CUDADenseGraphBFSearcher::searchRange,
+ * sqaodc/cuda/CUDADenseGraphBFSearcher.cpp:155-185).  Each tick searches the
+ * next 2^30 states of every active search (at most 4 at a time) on the
+ * searcher's own stream while the tick's anneals run; the result is the exact
+ * FP64 minimum and the minimisers in ascending packed order, at most tileSize
+ * of them, as sq103_dg_bf_search on the same W and tile_size returns them.
+ * Its sq103_server_result gives E[0] = the minimum (signed for `optimize`),
+ * *m = the number of minimisers and q0 = their bits x (0/1, one row of N each). */
+SQ103_API int sq103_server_submit_search(void *handle, const float *W, int N, int optimize, int tileSize, int *id);
+/* rows of the request's result: m for an anneal, the minimisers kept for a search */
+SQ103_API int sq103_server_result_rows(void *handle, int id, int *rows);
 /* E: m FP64 energies; q0 (m x N or m x N0) and q1 (m x N1, bipartite) spins;
  * release != 0 frees the request's host record. */
 SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int *m, int8_t *q0, int8_t *q1,

@@ -136,8 +136,8 @@ struct McShared {
     // exact decisions (rare): the decider posts a trial, the helper warp answers
     volatile int exReq;    // number of the latest request (decider)
     volatile int exDone;   // number of the latest answer (helper)
-    int exX, exBits;       // the trial's site; its FP64 outcomes for qL + qR = -2, 0, +2 (bits 0-2)
-    float exQ, exU, exG, exBeta;
+    int exX;               // the trial's site (every flip before the trial is in qs)
+    volatile double exF;   // its exact field (helper)
 };
 
 // every lane loads the flag with acquire semantics (one broadcast access); the
@@ -530,26 +530,29 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 if (lane == 0 && pending && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
             }
             if (exLane < 0 || aborted) break;
-            // The flagged lane's FP64 outcomes for each value of its neighbours' sum,
-            // computed by the helper warp from the exact field (every flip before the
-            // trial is in qs); the rounds then resume where they stopped.
-            if (lane == exLane) {
-                const int sl = (g0 + lane) / N;
-                S.exX = x;
-                S.exQ = qx;
-                S.exU = u;
-                S.exG = T.G ? T.G[sl] : T.Gs;
-                S.exBeta = T.beta ? T.beta[sl] : T.betas;
-            }
+            // The flagged lane's FP64 outcomes for each value of its neighbours' sum:
+            // the helper warp sums the trial's exact field (every flip before the trial
+            // is in qs) while lanes 0-2 evaluate the step's ring coefficient; lane k
+            // then decides the trial for the sum 2k - 2.  The rounds resume where
+            // they stopped.
+            const int xE = __shfl_sync(FULL, x, exLane);
+            if (lane == 0) S.exX = xE;
             ++exSeq;
             __syncwarp();
             if (lane == 0) st_release_cta(&S.exReq, exSeq);
+            const float qE = __shfl_sync(FULL, qx, exLane), uE = __shfl_sync(FULL, u, exLane);
+            const int slE = (g0 + exLane) / N;
+            const float GE = T.G ? T.G[slE] : T.Gs, bE = T.beta ? T.beta[slE] : T.betas;
+            const double hE = T.h64 ? T.h64[xE] : (double)hs[xE];
+            const double coefE = (!sa && lane < 3) ? exact_ring_coef(GE, bE, m) : 0.0;
             if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) {
                 aborted = true;
                 break;
             }
+            const int okE = lane < 3 ? exact_accept_coef(sa, true, qE, hE, S.exF, 2 * lane - 2, m, GE, bE, coefE, uE) : 0;
+            const unsigned bitsE = __ballot_sync(FULL, okE) & 7u;
             if (lane == exLane) {
-                exBits = S.exBits;
+                exBits = (int)bitsE;
                 exValid = true;
             }
             exLane = -1;
@@ -637,17 +640,10 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             if (req != served) {
                 served = req;
                 const int xr = S.exX;
-                const float qr = S.exQ, ur = S.exU, Gr = S.exG, br = S.exBeta;
-                const double hr = T.h64 ? T.h64[xr] : (double)hs[xr];
                 const double F = T.J64 ? exact_field_warp(T.J64 + (size_t)xr * N, qs, N)
                                        : exact_field_warp(T.J + (size_t)xr * T.ldJ, qs, N);
                 if (lane == 0) {
-                    int bits = 0;
-                    for (int k = 0; k < 3; ++k) {
-                        const float qL = k == 0 ? -1.f : 1.f, qR = k == 2 ? 1.f : -1.f;  // sum -2, 0, +2
-                        bits |= exact_accept(sa, true, qr, hr, F, qL, qR, m, Gr, br, ur) << k;
-                    }
-                    S.exBits = bits;
+                    S.exF = F;
                     st_release_cta(&S.exDone, req);
                 }
                 __syncwarp();

@@ -16,7 +16,12 @@
 //     does, so each instance ends exactly as it would alone.
 // Finished instances get their FP64 energies and spins copied out, and their
 // slot and memory are released in the same tick, so a waiting request can be
-// admitted by the next tick.  No counterpart in the reference.
+// admitted by the next tick.
+// Dense brute-force searches are served too: each tick searches the next 2^30
+// packed states of every active search with the single-instance searcher's own
+// range search (its own stream, so the sub-range runs while the tick's anneals
+// do), and a search that reaches 2^N completes with its exact minimum and
+// minimisers.  No counterpart in the reference.
 #include <algorithm>
 #include <cstring>
 #include <deque>
@@ -40,6 +45,9 @@ public:
     // take the per-instance path (GEMMs over the whole GPU) instead of one CTA
     static constexpr size_t kBipLargeWork = (size_t)1 << 22;
     enum State { kQueued = 0, kActive = 1, kDone = 2 };
+    enum Kind { kDenseAnneal = 0, kBipartiteAnneal = 1, kSearch = 2 };
+    static constexpr uint64_t kSearchChunk = 1ull << 30;  // states per search per tick
+    static constexpr int kMaxSearches = 4;                 // active searches
 
     // device memory of one request, allocated and freed in stream order (no
     // device-wide synchronisation per request)
@@ -100,7 +108,7 @@ public:
     };
 
     struct Request {
-        int id, kind;  // 0 dense, 1 bipartite
+        int id, kind;  // Kind
         int N0, N1, m, optimize, nSteps;
         unsigned long long seed;
         std::vector<float> W, b0, b1, G, beta;
@@ -120,9 +128,16 @@ public:
         void *digits = nullptr;        // tensor-core refresh of a dense request with N >= 1024
         void *spinsBf16 = nullptr;
         int status = 0;                // its value once the request is done
+        // a search: the searcher handle, the next state to search, 2^N, the list cap
+        void *bf = nullptr;
+        uint64_t xNext = 0, xMax = 0;
+        int tile = 0;
         // results
         std::vector<double> E;
         std::vector<int8_t> q0, q1;
+        ~Request() {
+            if (bf) sq103_dg_bf_delete(bf);
+        }
     };
 
     Server(unsigned long long budget, int maxSlots) : budget_(budget), maxSlots_(maxSlots) {
@@ -183,8 +198,22 @@ public:
         return enqueue(std::move(rq), m, optimize, seed, G, beta, nSteps);
     }
 
-    // kStepsPerTick steps (one refresh period) of every active instance; returns the
-    // number of requests completed
+    int submitSearch(const float *W, int N, int optimize, int tileSize) {
+        throwErrorIf(N <= 0 || N > 63, "a search needs 0 < N < 64, N=%d.", N);
+        throwErrorIf(tileSize <= 0, "tile size must be positive.");
+        throwErrorIf(!sqaod::isSymmetric(W, (size_t)N, (size_t)N), "%s, Matrix is not symmetric.", __func__);
+        auto rq = std::make_unique<Request>();
+        rq->kind = kSearch;
+        rq->N0 = N;
+        rq->N1 = 0;
+        rq->tile = tileSize;
+        rq->W.assign(W, W + (size_t)N * N);
+        const float none = 0.f;
+        return enqueue(std::move(rq), 1, optimize, 0, &none, &none, 1);
+    }
+
+    // kStepsPerTick steps (one refresh period) of every active instance and the
+    // next range of every active search; returns the number of requests completed
     int tick() {
         const int nDone = finalizeReady(false);
         admit();
@@ -241,11 +270,27 @@ public:
             if (r->pos >= r->nSteps) finished.push_back(r);
         }
         for (Request *r : finished) finish(r);
+        // searches: the next range of each, on the searcher's stream (the anneals
+        // queued above run meanwhile)
+        int nSearched = 0;
+        for (size_t i = 0; i < searches_.size();) {
+            Request *r = searches_[i];
+            const uint64_t e = std::min<uint64_t>(r->xMax, r->xNext + kSearchChunk);
+            bfCheck(sq103_dg_bf_search_subrange(r->bf, r->xNext, e));
+            r->xNext = e;
+            if (e < r->xMax) {
+                ++i;
+                continue;
+            }
+            searches_.erase(searches_.begin() + i);
+            finishSearch(r);
+            ++nSearched;
+        }
         ++ticks_;
         // nothing left to step (queued requests wait for memory or slots that only
         // collected results free): wait for the results still being computed
-        if (active_.size() == finishing_.size()) return nDone + finalizeReady(true);
-        return nDone;
+        if (active_.size() == finishing_.size()) return nDone + nSearched + finalizeReady(true);
+        return nDone + nSearched;
     }
 
     int state(int id) const {
@@ -291,6 +336,12 @@ public:
         maxLarge_ = n;
     }
 
+    int rows(int id) const {
+        const Request &r = request(id);
+        throwErrorIf(r.state != kDone, "request %d is not done.", id);
+        return r.kind == kSearch ? (int)(r.q0.size() / (size_t)r.N0) : r.m;
+    }
+
     void stats(int *queued, int *active, int *done, unsigned long long *bytes) const {
         if (queued) *queued = (int)queue_.size();
         if (active) *active = (int)active_.size();
@@ -322,6 +373,11 @@ private:
 
     static size_t footprint(const Request &r) {
         size_t s = 8 * 256 + al(r.nSteps * 4) * 2;
+        if (r.kind == kSearch) {
+            // the searcher's couplings, workspace and candidate buffers
+            const size_t N = r.N0, cap = std::min<size_t>(std::max<size_t>((size_t)r.tile, 1u << 16), 1u << 22);
+            return s + al(N * N * 4) + al(sq103_bf_workspace_bytes((int)N)) + 2 * al(cap * 8);
+        }
         if (r.kind == 0) {
             size_t N = r.N0, m = r.m;
             s += al(N * ldj(N) * 4) + al(N * 4) + al(m * N * 4) + al(m * N) + al(m * N * 8);
@@ -353,13 +409,15 @@ private:
             Request *r = queue_[i];
             // bipartite requests whose fields the single-instance annealer computes on the
             // tensor cores take the per-instance kernels, which do the same
-            const bool large = r->kind == 0 ? !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring)
-                                            : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork ||
-                                                  sq103_bipartite_refresh_uses_tc(r->N0, r->N1);
+            const bool large = r->kind == kSearch ? false
+                               : r->kind == 0 ? !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring)
+                                              : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork ||
+                                                    sq103_bipartite_refresh_uses_tc(r->N0, r->N1);
             const bool fits =
                 used_ + r->bytes <= budget_ &&
-                (large ? (int)large_.size() < maxLarge_  // each steps with the whole GPU every tick
-                       : (int)(r->kind == 0 ? denseSlots_.size() : bipSlots_.size()) < maxSlots_);
+                (r->kind == kSearch ? (int)searches_.size() < kMaxSearches
+                 : large            ? (int)large_.size() < maxLarge_  // each steps with the whole GPU every tick
+                                    : (int)(r->kind == 0 ? denseSlots_.size() : bipSlots_.size()) < maxSlots_);
             if (!fits) {
                 ++i;
                 continue;
@@ -379,8 +437,28 @@ private:
         }
     }
 
+    static void bfCheck(int rc) {
+        if (rc != 0) sqaod::throwError("search: %s", sq103_last_error());
+    }
+
     void setup(Request *r) {
         const int m = r->m, n = r->nSteps;
+        if (r->kind == kSearch) {
+            // the single-instance searcher with the request's tile size: its range
+            // searches give the result a whole search gives
+            bfCheck(sq103_dg_bf_new(&r->bf));
+            bfCheck(sq103_dg_bf_set_qubo(r->bf, r->W.data(), r->N0, r->optimize));
+            char tile[32];
+            snprintf(tile, sizeof(tile), "%d", r->tile);
+            bfCheck(sq103_dg_bf_set_preference(r->bf, "tile_size", tile));
+            bfCheck(sq103_dg_bf_prepare(r->bf));
+            r->xNext = 0;
+            r->xMax = 1ull << r->N0;
+            searches_.push_back(r);
+            r->W.clear();
+            r->W.shrink_to_fit();
+            return;
+        }
         if (r->kind == 0) {
             const size_t N = r->N0;
             const size_t ldJ = ldj(N);  // rows padded to 16 bytes for the one-CTA-per-trotter sweep
@@ -521,6 +599,27 @@ private:
         finishing_.push_back(r);
     }
 
+    // A search that has covered its 2^N states: its minimum and minimisers out,
+    // the searcher released, done in this tick.
+    void finishSearch(Request *r) {
+        bfCheck(sq103_dg_bf_make_solution(r->bf));
+        double E = 0.;
+        bfCheck(sq103_dg_bf_get_E64(r->bf, &E));
+        int n = 0;
+        bfCheck(sq103_dg_bf_solution_count(r->bf, &n));
+        r->E.assign(1, E);
+        r->q0.assign((size_t)std::max(n, 0) * r->N0, 0);
+        int got = 0;
+        if (n > 0) bfCheck(sq103_dg_bf_get_x(r->bf, r->q0.data(), n, &got));
+        bfCheck(sq103_dg_bf_delete(r->bf));
+        r->bf = nullptr;
+        used_ -= r->bytes;
+        active_.erase(r->id);
+        r->state = kDone;
+        completed_.push_back(r->id);
+        ++done_;
+    }
+
     // Collects, in completion order, the requests whose energies are done (all
     // of them when wait): energies, spins and the status word are copied on the
     // result stream, which waits only for that request's event, and its memory
@@ -594,7 +693,7 @@ private:
     std::deque<Request *> queue_;
     std::deque<int> completed_;
     std::map<int, Request *> active_;
-    std::vector<Request *> denseSlots_, bipSlots_, large_;
+    std::vector<Request *> denseSlots_, bipSlots_, large_, searches_;
     std::deque<Request *> finishing_;  // last step queued, results not yet collected
     DevBuf<sq103_dense_task> dTasks_;
     DevBuf<sq103_bipartite_task> bTasks_;
@@ -654,6 +753,19 @@ SQ103_API int sq103_server_submit_bipartite(void *h, const float *b0, const floa
         if (id) *id = i;
     });
 }
+SQ103_API int sq103_server_submit_search(void *h, const float *W, int N, int optimize, int tileSize, int *id) {
+    return serve_guard([&] {
+        throwErrorIf(!W, "null argument");
+        int i = as_server(h)->submitSearch(W, N, optimize, tileSize);
+        if (id) *id = i;
+    });
+}
+SQ103_API int sq103_server_result_rows(void *h, int id, int *rows) {
+    return serve_guard([&] {
+        throwErrorIf(!rows, "null argument");
+        *rows = as_server(h)->rows(id);
+    });
+}
 SQ103_API int sq103_server_tick(void *h, int *completed) {
     return serve_guard([&] {
         int c = as_server(h)->tick();
@@ -677,7 +789,7 @@ SQ103_API int sq103_server_result(void *h, int id, double *E, int capE, int *m, 
         }
         throwErrorIf((int)r.E.size() > capE, "energy capacity %d is smaller than %d.", capE, (int)r.E.size());
         if (E) memcpy(E, r.E.data(), sizeof(double) * r.E.size());
-        if (m) *m = r.m;
+        if (m) *m = s->rows(id);
         throwErrorIf((long long)r.q0.size() > capBytes || (long long)r.q1.size() > capBytes, "spin capacity too small.");
         if (q0) memcpy(q0, r.q0.data(), r.q0.size());
         if (q1 && !r.q1.empty()) memcpy(q1, r.q1.data(), r.q1.size());

@@ -154,8 +154,9 @@ __device__ __forceinline__ StepConst step_const(int algo, int m, float G, float 
 __device__ __forceinline__ float neg_log_unit(float u) { return u > 0.f ? -logf(u) : __int_as_float(0x7f800000); }
 
 // The error bound of x = rate dE for a trial with field F: the field error is
-// taken as 2^-12 (|h| + |F| + 1) (dense fields enter dE as 2F, bipartite as F),
-// about 200 times the drift seen over the 8 steps between field refreshes; the
+// taken as 2^-16 (|h| + |F| + 1) (dense fields enter dE as 2F, bipartite as F),
+// about 25 times the largest drift seen over the 8 steps between field
+// refreshes (6e-6 at |F| ~ 10, a random walk of rank-1 update roundings); the
 // rest covers the rounding of the ring term, of x and of -ln u.
 struct DecisionTol {
     float kF, kC;  // x tolerance = kF (|h| + |F'| + 1) + kC + 2.4e-7 L, F' = 2F (dense) or F
@@ -163,7 +164,7 @@ struct DecisionTol {
 __device__ __forceinline__ DecisionTol decision_tol(bool sa, bool dense, float twoDivM, float coef, float rate) {
     DecisionTol t;
     const float dF = sa ? 2.f : twoDivM;  // d(dE) / d(h + F')
-    t.kF = __fmul_rn(__fmul_rn(rate, dF), 2.44140625e-4f);
+    t.kF = __fmul_rn(__fmul_rn(rate, dF), 1.52587890625e-5f);
     t.kC = __fadd_rn(__fmul_rn(__fmul_rn(rate, 1e-6f), fabsf(coef)), 2e-6f);
     (void)dense;
     return t;
@@ -248,6 +249,69 @@ static __device__ __noinline__ double exact_field_warp(const R *Jx, const int8_t
     return exact_value(s, S);
 }
 
+// fp32 rows on a 16-byte boundary are read as float4 with eight loads in flight
+// per lane (the row of N = 4096 in four rounds); the second pass finds the row
+// in L1.  The same integer sum as the generic form.
+template <>
+__device__ __noinline__ double exact_field_warp<float>(const float *Jx, const int8_t *q, int N) {
+    typedef ExactFx<float> X;
+    const int lane = threadIdx.x & 31;
+    const bool vec = (reinterpret_cast<uintptr_t>(Jx) & 15) == 0 && (reinterpret_cast<uintptr_t>(q) & 3) == 0;
+    const int n4 = vec ? N / 4 : 0;
+    const float4 *J4 = reinterpret_cast<const float4 *>(Jx);
+    const char4 *q4 = reinterpret_cast<const char4 *>(q);
+    unsigned e = 0;
+#pragma unroll 8
+    for (int c = lane; c < n4; c += 32) {
+        const float4 v = __ldg(J4 + c);
+        e = max(e, max(max(X::expo(v.x), X::expo(v.y)), max(X::expo(v.z), X::expo(v.w))));
+    }
+    for (int j = 4 * n4 + lane; j < N; j += 32) e = max(e, X::expo(__ldg(Jx + j)));
+    e = __reduce_max_sync(0xffffffffu, e);
+    const int S = X::shift(e, log2_ceil(N));
+    long long s = 0;
+#pragma unroll 8
+    for (int c = lane; c < n4; c += 32) {
+        const float4 v = __ldg(J4 + c);
+        const char4 qq = q4[c];
+        const long long a = X::term(v.x, S), b = X::term(v.y, S), cc = X::term(v.z, S), d = X::term(v.w, S);
+        s += (qq.x > 0 ? a : -a) + (qq.y > 0 ? b : -b) + (qq.z > 0 ? cc : -cc) + (qq.w > 0 ? d : -d);
+    }
+    for (int j = 4 * n4 + lane; j < N; j += 32) {
+        const long long v = X::term(__ldg(Jx + j), S);
+        s += q[j] > 0 ? v : -v;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return exact_value(s, S);
+}
+
+// The FP64 ring coefficient log(tanh(G beta / m)) / beta of a step (SQA only)
+__device__ __forceinline__ double exact_ring_coef(float G, float beta, int m) {
+    const double Gd = G, bd = beta;
+    return log(tanh(__dmul_rn(Gd, bd) / (double)m)) / bd;
+}
+
+// exact_accept with the step's ring coefficient already evaluated (exact_ring_coef;
+// ignored for SA) and the neighbours' spin sum qL + qR given as `sum`
+__device__ __forceinline__ int exact_accept_coef(bool sa, bool twoF, float q, double h, double F, int sum, int m,
+                                                 float G, float beta, double coef, float u) {
+    const double qd = q, Gd = G, bd = beta;
+    const double t = __dadd_rn(h, twoF ? __dmul_rn(2.0, F) : F);
+    double dE, rate;
+    if (sa) {
+        dE = __dmul_rn(__dmul_rn(2.0, qd), t);
+        rate = 1.0 / Gd;
+    } else {
+        const double a = __dmul_rn(__dmul_rn(2.0 / (double)m, qd), t);
+        const double b = __dmul_rn(__dmul_rn(qd, (double)sum), coef);
+        dE = __dsub_rn(a, b);
+        rate = bd;
+    }
+    if (dE < 0.0) return 1;
+    return exp(__dmul_rn(-dE, rate)) > (double)u ? 1 : 0;
+}
+
 // FP64 decision of a dense trial from its exact field F, in the host replay's
 // order of operations: SQA dE = (2/m) q (h + 2F) - q (qL + qR) coef with
 // coef = log(tanh(G beta / m)) / beta, rate beta; SA dE = 2 q (h + 2F), rate 1/G;
@@ -255,21 +319,8 @@ static __device__ __noinline__ double exact_field_warp(const R *Jx, const int8_t
 // pass twoF = false.
 static __device__ __noinline__ int exact_accept(bool sa, bool twoF, float q, double h, double F, float qL, float qR,
                                                 int m, float G, float beta, float u) {
-    const double qd = q, hd = h, Gd = G, bd = beta;
-    const double t = __dadd_rn(hd, twoF ? __dmul_rn(2.0, F) : F);
-    double dE, rate;
-    if (sa) {
-        dE = __dmul_rn(__dmul_rn(2.0, qd), t);
-        rate = 1.0 / Gd;
-    } else {
-        const double coef = log(tanh(__dmul_rn(Gd, bd) / (double)m)) / bd;
-        const double a = __dmul_rn(__dmul_rn(2.0 / (double)m, qd), t);
-        const double b = __dmul_rn(__dmul_rn(qd, (double)((int)qL + (int)qR)), coef);
-        dE = __dsub_rn(a, b);
-        rate = bd;
-    }
-    if (dE < 0.0) return 1;
-    return exp(__dmul_rn(-dE, rate)) > (double)u ? 1 : 0;
+    const double coef = sa ? 0.0 : exact_ring_coef(G, beta, m);
+    return exact_accept_coef(sa, twoF, q, h, F, (int)qL + (int)qR, m, G, beta, coef, u);
 }
 #endif
 

@@ -1,4 +1,4 @@
-"""Request server: continuous batching of anneal requests of mixed size and type.
+"""Request server: continuous batching of anneal and search requests of mixed size and type.
 
 Requests (dense or bipartite QUBOs, each with its own trotter count, seed and
 G/beta schedule) are admitted in arrival order while their device-memory
@@ -11,7 +11,13 @@ A request with m > 1 trotters runs SQA with the coloring sweep; m == 1 runs
 simulated annealing (sa_naive for dense, sa_coloring for bipartite).  Each
 ends in exactly the state the single-instance annealer of
 sqaod_gb300.cuda reaches with the same algorithm, seed and schedule (after
-prepare() and randomize_spin()).  No counterpart in the reference.
+prepare() and randomize_spin()).
+
+Dense brute-force searches (N < 64) are served beside the anneals: each tick
+searches the next 2^30 states of every active search, and a finished search
+gives the exact FP64 minimum and its minimisers, as the single-instance
+searcher's search() with the same tile_size does.  No counterpart in the
+reference.
 """
 import ctypes
 
@@ -79,6 +85,19 @@ class AnnealServer:
         self._shape[rid.value] = (int(n_trotters), len(b0), len(b1))
         return rid.value
 
+    def submit_search(self, W, optimize=common.minimize, tile_size=1 << 18):
+        """Queues a dense brute-force search (W symmetric, or triangular as in
+        set_qubo, N < 64); returns its request id.  tile_size caps the number of
+        minimisers returned, as the searcher's preference of that name does."""
+        common.check_square(W)
+        W = common.fix_type(W, np.float32)
+        rid = ctypes.c_int()
+        common.submit_symmetric(W, np.float32, lambda w: self._call(
+            "submit_search", ptr(w), ctypes.c_int(w.shape[0]), ctypes.c_int(common.optimize_flag(optimize)),
+            ctypes.c_int(int(tile_size)), ctypes.byref(rid)))
+        self._shape[rid.value] = ("search", W.shape[0])
+        return rid.value
+
     def tick(self):
         """8 annealOneSteps of every active request; returns how many finished."""
         c = ctypes.c_int()
@@ -122,8 +141,12 @@ class AnnealServer:
         return ids[:n.value].tolist()
 
     def result(self, rid, release=True):
-        """(E, q) of a finished request: m FP64 energies and the spins, q of
-        shape (m, N) for dense or a pair ((m, N0), (m, N1)) for bipartite."""
+        """(E, q) of a finished anneal: m FP64 energies and the spins, q of
+        shape (m, N) for dense or a pair ((m, N0), (m, N1)) for bipartite.
+        (E, x) of a finished search: the FP64 minimum and its minimisers, x of
+        shape (n, N) with bits 0/1."""
+        if self._shape[rid][0] == "search":
+            return self._search_result(rid, release)
         m, N0, N1 = self._shape[rid]
         E = np.zeros(m, np.float64)
         q0 = np.zeros((m, N0), np.int8)
@@ -140,6 +163,20 @@ class AnnealServer:
         if N1 == 0:
             return E, q0
         return E, (q0, q1[:, :N1])
+
+    def _search_result(self, rid, release):
+        N = self._shape[rid][1]
+        rows = ctypes.c_int()
+        self._call("result_rows", ctypes.c_int(rid), ctypes.byref(rows))
+        n = rows.value
+        E = np.zeros(1, np.float64)
+        x = np.zeros((max(n, 1), N), np.int8)
+        got = ctypes.c_int()
+        self._call("result", ctypes.c_int(rid), ptr(E), ctypes.c_int(1), ctypes.byref(got), ptr(x), ptr(x),
+                   ctypes.c_longlong(x.nbytes), ctypes.c_int(1 if release else 0))
+        if release:
+            self._shape.pop(rid, None)
+        return float(E[0]), x[:n]
 
     def run(self, max_ticks=None):
         """Ticks until nothing is queued or active; returns the number of ticks."""

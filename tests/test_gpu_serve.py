@@ -204,3 +204,59 @@ def test_server_status_is_per_request():
     E, q = srv.result(late)
     E1, q1 = _alone(sq, specs[1], data[1], 4001)
     assert np.array_equal(E, E1) and np.array_equal(q, np.array(q1))
+
+
+def _search_alone(sq, W, opt, tile):
+    s = sq.cuda.dense_graph_bf_searcher(W, opt, tile_size=tile)
+    s.search()
+    return s.get_E64(), np.array(s.get_x())
+
+
+def test_server_searches_match_alone():
+    """Brute-force searches served beside anneals (some submitted between
+    ticks, one larger than a tick's 2^30 states): each gives the exact minimum
+    and the same minimisers, in the same order, as the single-instance search;
+    the anneals still match theirs."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import DONE, AnnealServer
+    rng = np.random.default_rng(51)
+
+    def int_sym(N, lo=-3, hi=4):
+        U = np.triu(rng.integers(lo, hi, (N, N)))
+        return (U + np.triu(U, 1).T).astype(np.float32)
+
+    # (W, optimize, tile_size): integer couplings give ties, so the lists have many entries
+    searches = [(int_sym(12), sq.minimize, 1 << 18), (int_sym(20, 0, 2), sq.maximize, 1 << 18),
+                (int_sym(16, -1, 2), sq.minimize, 5), (_sym(rng, 24), sq.minimize, 1 << 18),
+                (int_sym(31), sq.minimize, 1 << 18)]
+    srv = AnnealServer(budget_bytes=1 << 30)
+    G, beta = _schedule(16)
+    spec_a = ("d", 256, 8, 16, "min")
+    Wa = _sym(rng, 256)
+    ida = srv.submit_dense(Wa, 8, G, beta, sq.minimize, seed=5000)
+    ids = [srv.submit_search(W, o, tile_size=t) for W, o, t in searches[:2]]
+    srv.tick()
+    ids += [srv.submit_search(W, o, tile_size=t) for W, o, t in searches[2:]]
+    assert srv.run(max_ticks=100) < 100
+    for (W, o, t), rid in zip(searches, ids):
+        assert srv.state(rid) == DONE
+        E, x = srv.result(rid)
+        E1, x1 = _search_alone(sq, W, o, t)
+        assert E == E1, (E, E1)
+        assert np.array_equal(x, x1), (x.shape, x1.shape)
+        assert len(x) <= t and len(x) >= 1
+    E, q = srv.result(ida)
+    E1, q1 = _alone(sq, spec_a, Wa, 5000)
+    assert np.array_equal(E, E1) and np.array_equal(q, np.array(q1))
+
+
+def test_server_rejects_bad_search():
+    from sqaod_gb300._lib import SqaodError
+    from sqaod_gb300.serve import AnnealServer
+    srv = AnnealServer(budget_bytes=1 << 30)
+    with pytest.raises(SqaodError, match="0 < N < 64"):
+        srv.submit_search(np.zeros((64, 64), np.float32))
+    W = np.arange(9, dtype=np.float32).reshape(3, 3)
+    with pytest.raises(SqaodError):
+        srv.submit_search(W + W.T + np.array([[0, 1, 0], [0, 0, 0], [0, 0, 0]], np.float32))
+    assert srv.stats()["queued"] == 0
