@@ -332,26 +332,54 @@ def _solve_plain(sq, req, G):
     return a.get_E64()
 
 
+def _stratified_time(items, cost, solve, n_strata=16, per=3, seed=7):
+    """Estimated sequential time of solve() over every item: the items sorted by
+    cost, split into n_strata strata of equal count, `per` items drawn at random
+    from each and timed; the estimate is sum over strata of (count x mean time),
+    with its standard error from the within-stratum spread."""
+    order = sorted(range(len(items)), key=lambda i: cost(items[i]))
+    rng = np.random.default_rng(seed)
+    total, var, timed = 0.0, 0.0, {}
+    for st in np.array_split(np.array(order), n_strata):
+        if len(st) == 0:
+            continue
+        pick = rng.choice(st, size=min(per, len(st)), replace=False)
+        ts = []
+        for i in pick:
+            t1 = time.perf_counter()
+            timed[int(i)] = solve(items[int(i)])
+            ts.append(time.perf_counter() - t1)
+        total += len(st) * float(np.mean(ts))
+        if len(ts) > 1:
+            var += len(st) ** 2 * float(np.var(ts, ddof=1)) / len(ts)
+    return total, var ** 0.5, timed
+
+
+def _request_cost(r):
+    return (r["sizes"][0] ** 2 if r["dense"] else r["sizes"][0] * r["sizes"][1]) * r["m"]
+
+
 def run_served(args, world):
-    """C5: the served mixed stream against the plain path, each for a wall-time window."""
+    """C5: the whole seeded stream (Poisson arrivals over the window, 60 s by
+    default) submitted at its arrival times and served to the last completion;
+    solves/s = requests / makespan.  The plain path's time for the same stream
+    (one request after another on the single-instance solvers) is estimated from
+    a stratified sample of it, so both rates cover the same request mix."""
     import torch
     import sqaod_gb300 as sq
     from sqaod_gb300.serve import AnnealServer
-    reqs = served_stream()
+    reqs = served_stream(duration=args.window)
     G = schedule_1000()
-    T = args.window
     srv = AnnealServer(budget_bytes=180 << 30, max_slots=args.slots)
     srv.set_large_limit(args.large)
     ticks = 0
-    ids, arrival, finish = {}, {}, {}
+    ids, arrival, finish, served_E = {}, {}, {}, {}
     t_gen = t_submit = t_tick = 0.0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     k = 0
-    while True:
+    while len(finish) < len(reqs):
         now = time.perf_counter() - t0
-        if now >= T:
-            break
         while k < len(reqs) and reqs[k]["t"] <= now:
             ta = time.perf_counter()
             r, d = reqs[k], _couplings(reqs[k])
@@ -364,6 +392,11 @@ def run_served(args, world):
             t_submit += time.perf_counter() - tb
             ids[rid], arrival[rid] = k, r["t"]
             k += 1
+        s = srv.stats()
+        if s["queued"] == 0 and s["active"] == 0:
+            if k < len(reqs):  # idle until the next arrival
+                time.sleep(max(0.0, min(0.01, reqs[k]["t"] - (time.perf_counter() - t0))))
+            continue
         tc = time.perf_counter()
         nc = srv.tick()
         t_tick += time.perf_counter() - tc
@@ -372,41 +405,35 @@ def run_served(args, world):
             t_now = time.perf_counter() - t0
             for rid in srv.completed():
                 finish[rid] = t_now
-    served_E = {}
-    for rid in list(finish)[:args.check]:
-        served_E[ids[rid]] = srv.result(rid)[0]
+                E = srv.result(rid)[0]  # released at once; energies kept for the check
+                served_E[ids[rid]] = E
+    makespan = max(finish.values())
     lat = sorted(finish[r] - arrival[r] for r in finish)
-    served = {"solves": len(finish), "window_s": T, "solves_per_s": len(finish) / T, "submitted": k,
-              "ticks": ticks, "ms_per_tick": 1000.0 * T / max(ticks, 1),
+    served = {"solves": len(finish), "makespan_s": makespan, "solves_per_s": len(finish) / makespan,
+              "stream_s": args.window, "ticks": ticks, "ms_per_tick": 1000.0 * makespan / max(ticks, 1),
               "host_s": {"generate_couplings": t_gen, "submit": t_submit, "tick": t_tick},
-              "p50_s": lat[len(lat) // 2] if lat else None,
-              "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None}
+              "p50_s": lat[len(lat) // 2], "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))]}
     del srv
-    # the plain path: the same requests, in arrival order, one at a time
-    t0 = time.perf_counter()
-    done, plain_E, lat_p = 0, {}, []
-    while time.perf_counter() - t0 < T and done < len(reqs):
-        E = _solve_plain(sq, reqs[done], G)
-        if done in served_E:
-            plain_E[done] = E
-        lat_p.append(time.perf_counter() - t0 - reqs[done]["t"])
-        done += 1
-    tp = time.perf_counter() - t0
-    lat_p.sort()
-    plain = {"solves": done, "window_s": tp, "solves_per_s": done / tp,
-             "p50_s": lat_p[len(lat_p) // 2] if lat_p else None,
-             "p99_s": lat_p[min(len(lat_p) - 1, int(0.99 * len(lat_p)))] if lat_p else None}
+    # the plain path over the same stream, from a stratified sample of it
+    t_est, t_se, plain_E = _stratified_time(reqs, _request_cost, lambda r: _solve_plain(sq, r, G),
+                                            n_strata=16, per=args.plain_per_stratum)
+    plain = {"solves_per_s": len(reqs) / t_est, "seconds_estimated": t_est, "seconds_std_error": t_se,
+             "sample": len(plain_E),
+             "note": "requests sorted by N^2 m (dense) or N0 N1 m (bipartite), 16 strata of equal count, "
+                     "%d timed per stratum on the single-instance solvers (set_qubo, prepare, anneal, "
+                     "make_solution, energies); time = sum of count x mean" % args.plain_per_stratum}
     rel = [float(np.max(np.abs(served_E[i] - plain_E[i]) / np.maximum(np.abs(plain_E[i]), 1e-30)))
            for i in plain_E]
     line = {"metric": "served vs plain solves/s (mixed stream)", "value": served["solves_per_s"],
             "unit": "solves/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Poisson stream, uniform[-1,1] couplings)",
-            "config": {"workload": ("Poisson 200 req/s, 70 pct dense N log-uniform [32, 4096], 30 pct bipartite "
-                                    "N0/N1 log-uniform [32, 2048], m in {16, 64, 256}, 1000-step G 5.0 -> 0.01, "
-                                    "beta=50; served and plain each for a %.0f s wall-time window") % T,
+            "config": {"workload": ("Poisson 200 req/s over %.0f s (%d requests), 70 pct dense N log-uniform "
+                                    "[32, 4096], 30 pct bipartite N0/N1 log-uniform [32, 2048], m in {16, 64, 256}, "
+                                    "1000-step G 5.0 -> 0.01, beta=50; every request served to completion")
+                                   % (args.window, len(reqs)),
                        "slots": args.slots, "large_limit": args.large, "admission_bytes": 180 << 30},
             "served": served, "plain": plain,
-            "served_over_plain": served["solves_per_s"] / max(plain["solves_per_s"], 1e-30),
+            "served_over_plain": served["solves_per_s"] / plain["solves_per_s"],
             "energy_check": {"requests": len(rel), "max_rel_diff": max(rel) if rel else None}}
     print(json.dumps(line), flush=True)
 
@@ -449,8 +476,9 @@ def run_batched(args, world):
     t_out = time.perf_counter() - t_out
     trials = float(sum(N * m for N, m, _ in work)) * steps
     t_total = t_add + t_batch + t_out
-    # plain path on a sample
-    sample = list(range(0, len(work), len(work) // args.plain_sample))[:args.plain_sample]
+    # plain path: every instance (--plain-sample 0, the default) or an evenly spaced sample
+    ns = len(work) if args.plain_sample <= 0 else args.plain_sample
+    sample = list(range(0, len(work), max(1, len(work) // ns)))[:ns]
     t_plain, rel = 0.0, []
     for i in sample:
         N, m, seed = work[i]
@@ -484,9 +512,10 @@ def run_batched(args, world):
                         "note": "seconds = the annealing launches alone; with_setup adds add()+prepare() of "
                                 "all instances and reading every instance's energies (autotune, a one-off, not)"},
             "plain": {"sample": len(sample), "seconds": t_plain, "trials_per_s": plain_tps,
+                      "solves_per_s": len(sample) / t_plain if len(sample) == len(work) else None,
                       "solves_per_s_extrapolated": len(work) / (trials / plain_tps),
-                      "note": "sequential single-instance solves of an evenly spaced sample (set_qubo, prepare, "
-                              "anneal, make_solution, energies), extrapolated by trials"},
+                      "note": "sequential single-instance solves (set_qubo, prepare, anneal, make_solution, "
+                              "energies) of every instance, or of an evenly spaced sample extrapolated by trials"},
             "batched_over_plain": (trials / t_batch) / plain_tps,
             "batched_over_plain_with_setup": (trials / t_total) / plain_tps,
             "energy_check": {"instances": len(rel), "max_rel_diff": max(rel) if rel else None}}
@@ -772,13 +801,16 @@ def main():
     ap.add_argument("--mode", default="sweep", choices=["sweep", "batched", "served", "bipartite", "bf"],
                     help="sweep: the headline dense sweep; batched: 1024 uneven instances; served: mixed stream; "
                          "bipartite: N0=N1=1024 m=64 sweep; bf: dense brute force N=32")
-    ap.add_argument("--window", type=float, default=20.0, help="served mode: seconds per path")
+    ap.add_argument("--window", type=float, default=60.0, help="served mode: seconds of Poisson arrivals")
+    ap.add_argument("--plain-per-stratum", type=int, default=3,
+                    help="served mode: plain solves timed per stratum of the stream (16 strata)")
     ap.add_argument("--slots", type=int, default=512, help="served mode: concurrent instances per kind")
     ap.add_argument("--large", type=int, default=8,
                     help="served mode: concurrent large instances (dense ones step together in packed launches)")
     ap.add_argument("--check", type=int, default=16, help="served mode: requests compared with the plain path")
     ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")
-    ap.add_argument("--plain-sample", type=int, default=16, help="batched mode: instances solved on the plain path")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="batched mode: instances solved on the plain path (0: all of them)")
     ap.add_argument("--multicta-min-n", type=int, default=None,
                     help="batched mode: instances of at least this N take the one-CTA-per-trotter sweep (default 1024)")
     ap.add_argument("--cpu-leg", action="store_true", help="internal: time the CPU reference annealer alone")

@@ -200,6 +200,30 @@ __device__ __forceinline__ void window_bits(int x, int Ji, int j0, int pLast, in
     }
 }
 
+// Decider warp, out of line (the FP64 code stays out of the decision loop's
+// instruction stream): the FP64 outcomes of lane exLane's trial for each value
+// -2, 0, +2 of its neighbours' spin sum (bits 0-2).  The helper warp sums the
+// trial's exact field (every flip before the trial is in qs) while lanes 0-2
+// evaluate the step's ring coefficient; lane k then decides the trial for the
+// sum 2k - 2.  -1 when the wait for the helper runs out.
+static __device__ __noinline__ int exact_outcomes(McShared &S, const sq103_dense_task &T, const float *hs, bool sa,
+                                                  int m, int N, int g0, int exLane, int x, float qx, float u,
+                                                  int exSeq, unsigned long long waitNs) {
+    const int lane = threadIdx.x & 31;
+    const int xE = __shfl_sync(FULL, x, exLane);
+    if (lane == 0) S.exX = xE;
+    __syncwarp();
+    if (lane == 0) st_release_cta(&S.exReq, exSeq);
+    const float qE = __shfl_sync(FULL, qx, exLane), uE = __shfl_sync(FULL, u, exLane);
+    const int slE = (g0 + exLane) / N;
+    const float GE = T.G ? T.G[slE] : T.Gs, bE = T.beta ? T.beta[slE] : T.betas;
+    const double hE = T.h64 ? T.h64[xE] : (double)hs[xE];
+    const double coefE = (!sa && lane < 3) ? exact_ring_coef(GE, bE, m) : 0.0;
+    if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) return -1;
+    const int okE = lane < 3 ? exact_accept_coef(sa, true, qE, hE, S.exF, 2 * lane - 2, m, GE, bE, coefE, uE) : 0;
+    return (int)(__ballot_sync(FULL, okE) & 7u);
+}
+
 // Up to kMaxPack independent instances in one cooperative launch: CTAs
 // [base[i], base[i+1]) are the trotters of task t[i], whose accept words live in
 // outLog[i] (nWords[i] per trotter).  Instances do not interact (the prologue's
@@ -530,29 +554,15 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 if (lane == 0 && pending && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
             }
             if (exLane < 0 || aborted) break;
-            // The flagged lane's FP64 outcomes for each value of its neighbours' sum:
-            // the helper warp sums the trial's exact field (every flip before the trial
-            // is in qs) while lanes 0-2 evaluate the step's ring coefficient; lane k
-            // then decides the trial for the sum 2k - 2.  The rounds resume where
-            // they stopped.
-            const int xE = __shfl_sync(FULL, x, exLane);
-            if (lane == 0) S.exX = xE;
-            ++exSeq;
-            __syncwarp();
-            if (lane == 0) st_release_cta(&S.exReq, exSeq);
-            const float qE = __shfl_sync(FULL, qx, exLane), uE = __shfl_sync(FULL, u, exLane);
-            const int slE = (g0 + exLane) / N;
-            const float GE = T.G ? T.G[slE] : T.Gs, bE = T.beta ? T.beta[slE] : T.betas;
-            const double hE = T.h64 ? T.h64[xE] : (double)hs[xE];
-            const double coefE = (!sa && lane < 3) ? exact_ring_coef(GE, bE, m) : 0.0;
-            if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) {
+            // The flagged lane's FP64 outcomes for each value of its neighbours' sum;
+            // the rounds then resume where they stopped.
+            const int bitsE = exact_outcomes(S, T, hs, sa, m, N, g0, exLane, x, qx, u, ++exSeq, waitNs);
+            if (bitsE < 0) {
                 aborted = true;
                 break;
             }
-            const int okE = lane < 3 ? exact_accept_coef(sa, true, qE, hE, S.exF, 2 * lane - 2, m, GE, bE, coefE, uE) : 0;
-            const unsigned bitsE = __ballot_sync(FULL, okE) & 7u;
             if (lane == exLane) {
-                exBits = (int)bitsE;
+                exBits = bitsE;
                 exValid = true;
             }
             exLane = -1;

@@ -262,6 +262,7 @@ public:
         std::vector<Request *> finished;
         for (auto &kv : active_) {
             Request *r = kv.second;
+            if (r->kind == kSearch) continue;   // advanced below
             if (r->pos >= r->nSteps) continue;  // finishing: its results are being collected
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)

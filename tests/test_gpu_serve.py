@@ -257,6 +257,6 @@ def test_server_rejects_bad_search():
     with pytest.raises(SqaodError, match="0 < N < 64"):
         srv.submit_search(np.zeros((64, 64), np.float32))
     W = np.arange(9, dtype=np.float32).reshape(3, 3)
-    with pytest.raises(SqaodError):
+    with pytest.raises(RuntimeError, match="not triangular nor symmetric"):
         srv.submit_search(W + W.T + np.array([[0, 1, 0], [0, 0, 0], [0, 0, 0]], np.float32))
     assert srv.stats()["queued"] == 0
