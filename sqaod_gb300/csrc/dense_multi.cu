@@ -31,8 +31,11 @@
 //           sites and one hashed-site bitmap per batch), and per lane the
 //           neighbour iterations of this and the previous batch that hit its
 //           site, into a ring of kPre batch buffers with a ready tag each.
-//   warps 4-7 updaters: F[y][:] += d * J[x][:] for the flips of the previous
+//   warps 4-6 updaters: F[y][:] += d * J[x][:] for the flips of the previous
 //           batch, in trial order, while the decider works on the next one.
+//   warp 7  exact decisions: a trial whose fp32 outcome the rounding of the
+//           resident field could change is decided in FP64 from its exact field
+//           (sq_common.cuh); the warp sleeps on a named barrier between requests.
 // Colour order: trial (y, k) must see neighbour n after every neighbour trial
 // that precedes it (iteration < k, or = k when n's colour phase comes first:
 // even trotters, then trotter m-1 if m is odd, then odd trotters).  The
@@ -57,8 +60,10 @@ namespace sq103 {
 constexpr int kMcThreads = 256;
 constexpr int kPf = 2;                            // prefetcher warps (2 .. 1 + kPf)
 constexpr int kUpdWarp0 = 2 + kPf;                // first updater warp
-constexpr int kMcUpdaters = kMcThreads - 32 * kUpdWarp0;
-constexpr int kBarCount = 32 + kMcUpdaters;       // decider + updaters
+constexpr int kExactWarp = kMcThreads / 32 - 1;   // the last warp: exact decisions
+constexpr int kMcUpdaters = kMcThreads - 32 * kUpdWarp0 - 32;
+constexpr int kBarCount = 32 + kMcUpdaters;       // decider + updaters (barriers 1, 2)
+constexpr int kBarExReq = 3, kBarExDone = 4;      // decider + exact warp (64 threads)
 constexpr int kRing = 256;      // neighbour sites kept per neighbour (power of two)
 constexpr int kLogWords = 32;   // neighbour accept words kept per neighbour (power of two)
 constexpr int kBmBits = 2048;   // bits of a batch's neighbour-site bitmap (hashed sites, power of two)
@@ -133,11 +138,9 @@ struct McShared {
     volatile int decDone;                  // batches [0, decDone) no longer read from the buffers (decider)
     volatile int done;
     int nflip;
-    // exact decisions (rare): the decider posts a trial, the helper warp answers
-    volatile int exReq;    // number of the latest request (decider)
-    volatile int exDone;   // number of the latest answer (helper)
-    int exX;               // the trial's site (every flip before the trial is in qs)
-    volatile double exF;   // its exact field (helper)
+    // exact decisions (rare): the decider posts a trial, the exact warp answers
+    int exX, exBits;       // the trial's site; its FP64 outcomes for qL + qR = -2, 0, +2 (bits 0-2)
+    float exQ, exU, exG, exBeta;
 };
 
 // every lane loads the flag with acquire semantics (one broadcast access); the
@@ -200,30 +203,6 @@ __device__ __forceinline__ void window_bits(int x, int Ji, int j0, int pLast, in
     }
 }
 
-// Decider warp, out of line (the FP64 code stays out of the decision loop's
-// instruction stream): the FP64 outcomes of lane exLane's trial for each value
-// -2, 0, +2 of its neighbours' spin sum (bits 0-2).  The helper warp sums the
-// trial's exact field (every flip before the trial is in qs) while lanes 0-2
-// evaluate the step's ring coefficient; lane k then decides the trial for the
-// sum 2k - 2.  -1 when the wait for the helper runs out.
-static __device__ __noinline__ int exact_outcomes(McShared &S, const sq103_dense_task &T, const float *hs, bool sa,
-                                                  int m, int N, int g0, int exLane, int x, float qx, float u,
-                                                  int exSeq, unsigned long long waitNs) {
-    const int lane = threadIdx.x & 31;
-    const int xE = __shfl_sync(FULL, x, exLane);
-    if (lane == 0) S.exX = xE;
-    __syncwarp();
-    if (lane == 0) st_release_cta(&S.exReq, exSeq);
-    const float qE = __shfl_sync(FULL, qx, exLane), uE = __shfl_sync(FULL, u, exLane);
-    const int slE = (g0 + exLane) / N;
-    const float GE = T.G ? T.G[slE] : T.Gs, bE = T.beta ? T.beta[slE] : T.betas;
-    const double hE = T.h64 ? T.h64[xE] : (double)hs[xE];
-    const double coefE = (!sa && lane < 3) ? exact_ring_coef(GE, bE, m) : 0.0;
-    if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) return -1;
-    const int okE = lane < 3 ? exact_accept_coef(sa, true, qE, hE, S.exF, 2 * lane - 2, m, GE, bE, coefE, uE) : 0;
-    return (int)(__ballot_sync(FULL, okE) & 7u);
-}
-
 // Up to kMaxPack independent instances in one cooperative launch: CTAs
 // [base[i], base[i+1]) are the trotters of task t[i], whose accept words live in
 // outLog[i] (nWords[i] per trotter).  Instances do not interact (the prologue's
@@ -237,6 +216,9 @@ struct McPack {
     int n;
 };
 
+// kHooks: the test hooks of the task flags are compiled in (short waits, a
+// trotter that withholds its accept words); the production instance has none.
+template <bool kHooks>
 __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ McShared S;
@@ -282,8 +264,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
     const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
     // test hooks (task flags): every wait gives up after 1 ms; trotter 0 never
     // publishes its accept words, so its neighbours' waits run out
-    const unsigned long long waitNs = (T.flags & kFlagShortWaits) ? kShortWaitNs : kWaitLimitNs;
-    const bool publish = !((T.flags & kFlagWithholdTrotter0) && y == 0);
+    const unsigned long long waitNs = (kHooks && (T.flags & kFlagShortWaits)) ? kShortWaitNs : kWaitLimitNs;
+    const bool publish = !(kHooks && (T.flags & kFlagWithholdTrotter0) && y == 0);
 
     float *Fs = reinterpret_cast<float *>(smem);                        // N
     float *hs = Fs + N;                                                 // N
@@ -315,7 +297,6 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         }
     }
     if (tid == 0) {
-        S.exReq = S.exDone = 0;
         S.logAvail = 0;
         S.applied[0] = S.applied[1] = 0;
         for (int i = 0; i < kPre; ++i) S.readyTag[i] = 0;
@@ -340,7 +321,6 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         for (int t = 0; t < kGv; ++t) gv[t] = 0.f;
 
         int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
-        int exSeq = 0;       // exact-decision requests posted to the helper warp
 
         // Applies the published neighbour iterations below lim0 / lim1 (their sites
         // are in the ring) to the ghost rows; returns the helper's availability word.
@@ -465,10 +445,9 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
             float d = 0.f;
             bool exValid = false;  // exBits holds the FP64 outcomes of the lane's trial
             int exBits = 0;
-            int exLane = -1;       // a flagged lane whose trial waits for its exact decision
             const DecisionTol tolD = decision_tol(sa, true, sc.twoDivM, sc.coef, sc.rate);
+            float xt = trial_xtol(tolD, hx, __fmul_rn(2.f, Fv), Lu);  // updated when Fv changes
             bool evalNbr = nNbr > 0;  // (one instance of nbr_bits keeps the loop's code small)
-            for (;;) {
             while (pending) {
                 if (evalNbr) {
                     nbr_bits(b, g0, valid, avEval);
@@ -477,12 +456,12 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 }
                 // a lane with unknown neighbour bits is decided anyway when every value
                 // those bits can take gives the same outcome; it blocks otherwise.  The
-                // outcomes come from the fp32 field, flagged where its rounding could
-                // change them, or from the FP64 outcomes of a flagged lane's trial
+                // outcomes come from the fp32 field, or from the FP64 outcomes of a
+                // flagged lane's trial; a flagged lane (one whose fp32 outcome the field's
+                // rounding could change) blocks too, until it has its FP64 outcomes
                 int acc = 0, amb = 0, nearT = 0;
                 if ((pending >> lane) & 1u) {
                     const float qn0 = qb0 ? 1.f : -1.f, qn1 = nNbr == 1 ? qn0 : (qb1 ? 1.f : -1.f);
-                    const float xt = trial_xtol(tolD, hx, __fmul_rn(2.f, Fv), Lu);
                     auto accept = [&](float a, float c) -> int {
                         if (exValid) return (exBits >> (((int)a + (int)c + 2) >> 1)) & 1;
                         const float dE = sa ? dense_sa_dE(qx, hx, Fv)
@@ -497,24 +476,37 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                         if (u0 && u1 && accept(-qn0, -qn1) != acc) amb = 1;
                     }
                 }
+                amb |= nearT;
                 const unsigned accM = __ballot_sync(FULL, acc && !amb) & pending;
                 const unsigned blkM = __ballot_sync(FULL, amb) & pending;
-                const unsigned nearM = __ballot_sync(FULL, nearT) & pending;
-                if (nearM) {
-                    // a flagged lane that would be this round's first decision needs its
-                    // exact decision first (served below, outside the rounds)
-                    const int fl = __ffs(accM | blkM | nearM) - 1;
-                    if ((nearM >> fl) & 1u) {
-                        exLane = fl;
-                        break;
-                    }
-                }
                 const int fa = accM ? __ffs(accM) - 1 : 32;
                 const int fb = blkM ? __ffs(blkM) - 1 : 32;
                 if (fb < fa) {
-                    // undecided lanes below fb reject; fb waits for its neighbour trials
+                    // undecided lanes below fb reject
                     pending &= ~((1u << fb) - 1u);
                     if (lane == 0 && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fb, accBits));
+                    if (__shfl_sync(FULL, nearT, fb)) {
+                        // fb is flagged: the exact warp decides its trial in FP64 from the
+                        // exact field (every flip before the trial is in qs), for each value
+                        // of the neighbours' spin sum; then the round is evaluated again.
+                        // (Named barriers: no polling; the exact warp sleeps between requests.)
+                        if (lane == fb) {
+                            const int sl = (g0 + lane) / N;
+                            S.exX = x;
+                            S.exQ = qx;
+                            S.exU = u;
+                            S.exG = T.G ? T.G[sl] : T.Gs;
+                            S.exBeta = T.beta ? T.beta[sl] : T.betas;
+                        }
+                        bar_sync(kBarExReq, 64);
+                        bar_sync(kBarExDone, 64);
+                        if (lane == fb) {
+                            exBits = S.exBits;
+                            exValid = true;
+                        }
+                        continue;
+                    }
+                    // fb waits for its neighbour trials
                     const int w0 = __shfl_sync(FULL, nd0, fb), w1 = __shfl_sync(FULL, nd1, fb);
                     unsigned long long av = 0;
                     if (!wait_until(waitNs, [&] {
@@ -545,6 +537,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 if (lane > fa) {
                     const float jv = ((pred >> fa) & 1u) ? jg[fa] : __ldg(T.J + (size_t)xf * T.ldJ + x);
                     Fv = __fmaf_rn(df, jv, Fv);
+                    xt = trial_xtol(tolD, hx, __fmul_rn(2.f, Fv), Lu);
                     if (x == xf) qx = -qx;
                     exValid = false;  // the trial now follows another flip
                 }
@@ -552,20 +545,6 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 pending &= ~((2u << fa) - 1u);
                 // trials through fa are decided: make them visible to the neighbours
                 if (lane == 0 && pending && publish) st_relaxed_u64(outLog + (size_t)y * nWords + b, log_word(b, fa + 1, accBits));
-            }
-            if (exLane < 0 || aborted) break;
-            // The flagged lane's FP64 outcomes for each value of its neighbours' sum;
-            // the rounds then resume where they stopped.
-            const int bitsE = exact_outcomes(S, T, hs, sa, m, N, g0, exLane, x, qx, u, ++exSeq, waitNs);
-            if (bitsE < 0) {
-                aborted = true;
-                break;
-            }
-            if (lane == exLane) {
-                exBits = bitsE;
-                exValid = true;
-            }
-            exLane = -1;
             }
             if (aborted) break;
             __syncwarp();
@@ -636,32 +615,14 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         __syncwarp();
         __threadfence_block();
         bar_arrive(1, kBarCount);
+        bar_sync(kBarExReq, 64);  // the exact warp sees done and leaves
     } else if (warp == 1) {
         // -------------------------------------------------------------- helper
         // lane l < 4 polls word (avail[n] >> 5) + dw of neighbour n = l & 1, dw = l >> 1
-        int avail0 = 0, avail1 = 0, served = 0;
+        int avail0 = 0, avail1 = 0;
         const int n = lane & 1, dw = lane >> 1;
         const unsigned long long *nbLog = outLog + (size_t)(n ? nbr1 : nbr0) * nWords;
-        while (!__shfl_sync(FULL, (int)S.done, 0)) {
-            // an exact decision the decider waits for: the trial's exact field (the
-            // integer row sum, as the one-CTA kernel computes it) and its FP64 outcome
-            // for each value of the neighbours' sum
-            const int req = uniform_acquire(&S.exReq);
-            if (req != served) {
-                served = req;
-                const int xr = S.exX;
-                const double F = T.J64 ? exact_field_warp(T.J64 + (size_t)xr * N, qs, N)
-                                       : exact_field_warp(T.J + (size_t)xr * T.ldJ, qs, N);
-                if (lane == 0) {
-                    S.exF = F;
-                    st_release_cta(&S.exDone, req);
-                }
-                __syncwarp();
-            }
-            if (nNbr == 0) {
-                __nanosleep(64);
-                continue;
-            }
+        while (nNbr > 0 && !__shfl_sync(FULL, (int)S.done, 0)) {
             const int an = n ? avail1 : avail0;
             const int w = (an >> 5) + dw;
             unsigned long long v = 0;
@@ -691,6 +652,29 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                     st_release_cta64(&S.logAvail, (unsigned long long)(unsigned)avail0 |
                                                       ((unsigned long long)(unsigned)avail1 << 32));
             }
+        }
+    } else if (warp == kExactWarp) {
+        // --------------------------------------------------------- exact warp
+        // Sleeps on a named barrier until the decider posts a flagged trial: sums
+        // its exact field (the integer row sum, as the one-CTA kernel computes it)
+        // and decides it in FP64 for each value of the neighbours' spin sum (lane
+        // k < 3: the sum 2k - 2).
+        for (;;) {
+            bar_sync(kBarExReq, 64);
+            if (S.done) break;
+            const int xr = S.exX;
+            const float qr = S.exQ, ur = S.exU, Gr = S.exG, br = S.exBeta;
+            const double hr = T.h64 ? T.h64[xr] : (double)hs[xr];
+            const double F = T.J64 ? exact_field_warp(T.J64 + (size_t)xr * N, qs, N)
+                                   : exact_field_warp(T.J + (size_t)xr * T.ldJ, qs, N);
+            const int ok = lane < 3 ? exact_accept(sa, true, qr, hr, F, lane == 0 ? -1.f : 1.f, lane == 2 ? 1.f : -1.f,
+                                                   m, Gr, br, ur)
+                                    : 0;
+            const unsigned bits = __ballot_sync(FULL, ok) & 7u;
+            if (lane == 0) S.exBits = (int)bits;
+            __syncwarp();
+            __threadfence_block();
+            bar_arrive(kBarExDone, 64);
         }
     } else if (warp < kUpdWarp0) {
         // --------------------------------------------------------- prefetchers
@@ -946,17 +930,23 @@ static int multi_capacity(int N) {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     size_t smem = multi_smem_bytes(N);
     cudaFuncAttributes fa;
-    cudaFuncGetAttributes(&fa, dense_sweep_multi);
+    cudaFuncGetAttributes(&fa, dense_sweep_multi<false>);
     if (smem + fa.sharedSizeBytes > (size_t)optin) return 0;
-    if (cudaFuncSetAttribute(dense_sweep_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess) {
+    for (const void *k : {(const void *)dense_sweep_multi<false>, (const void *)dense_sweep_multi<true>})
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+    // both instances: the launch takes the one the tasks' flags ask for
+    int perSmHooks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_sweep_multi<false>, kMcThreads, smem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmHooks, dense_sweep_multi<true>, kMcThreads, smem) !=
+            cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_sweep_multi, kMcThreads, smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
+    perSm = std::min(perSm, perSmHooks);
     cachedN = N;
     cachedCap = perSm * sms;
     return cachedCap;
@@ -986,8 +976,10 @@ static int launch_pack(const sq103_dense_task *tasks, int n, void *stream) {
     McPack P = {};
     P.n = n;
     int maxN = 0, ctas = 0;
+    bool hooks = false;
     for (int i = 0; i < n; ++i) {
         const sq103_dense_task &t = tasks[i];
+        hooks |= (t.flags & (kFlagShortWaits | kFlagWithholdTrotter0)) != 0;
         const int N = t.N, m = t.m;
         if (t.algo != kColoring && t.algo != kSANaive) return kErrBadShape;
         if (N < 64 || m < 2 || t.nSteps < 1) return kErrBadShape;
@@ -1011,8 +1003,8 @@ static int launch_pack(const sq103_dense_task *tasks, int n, void *stream) {
         if (e != cudaSuccess) return (int)e;
     }
     void *args[] = {&P};
-    return (int)cudaLaunchCooperativeKernel((const void *)dense_sweep_multi, dim3(ctas), dim3(kMcThreads), args,
-                                           multi_smem_bytes(maxN), st);
+    const void *kernel = hooks ? (const void *)dense_sweep_multi<true> : (const void *)dense_sweep_multi<false>;
+    return (int)cudaLaunchCooperativeKernel(kernel, dim3(ctas), dim3(kMcThreads), args, multi_smem_bytes(maxN), st);
 }
 
 // launched from sq103_dense_anneal (dense.cu) when the shape and workspace allow it
