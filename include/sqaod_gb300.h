@@ -134,8 +134,9 @@ SQ103_API int sq103_tc_refresh(const void *digits, int R, int K, const int8_t *q
 /* 1 when the dense annealers refresh N-spin fields on the tensor cores (N >= 1024) */
 SQ103_API int sq103_dense_refresh_uses_tc(int N);
 /* 1 when the bipartite annealers compute the half-step fields on the tensor cores
- * (N0 N1 >= 2^20); the task then carries the digits of J and J^T */
-SQ103_API int sq103_bipartite_refresh_uses_tc(int N0, int N1);
+ * (N0 N1 >= 2^20 and at least 64 output tiles of 128 trotters x 64 spins per half
+ * step); the task then carries the digits of J and J^T */
+SQ103_API int sq103_bipartite_refresh_uses_tc(int N0, int N1, int m);
 /* the dense refresh of every path: sq103_tc_refresh from `digits` (of J, R = K = N)
  * when given, else sq103_dense_field_refresh */
 SQ103_API int sq103_dense_refresh(const float *J, int ldJ, const void *digits, void *spinsBf16, const int8_t *q,

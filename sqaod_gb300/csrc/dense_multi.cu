@@ -35,7 +35,8 @@
 //           batch, in trial order, while the decider works on the next one.
 //   warp 7  exact decisions: a trial whose fp32 outcome the rounding of the
 //           resident field could change is decided in FP64 from its exact field
-//           (sq_common.cuh); the warp sleeps on a named barrier between requests.
+//           (sq_common.cuh); the warp sleeps on a named barrier between requests
+//           and answers through a shared word the decider waits on (bounded).
 // Colour order: trial (y, k) must see neighbour n after every neighbour trial
 // that precedes it (iteration < k, or = k when n's colour phase comes first:
 // even trotters, then trotter m-1 if m is odd, then odd trotters).  The
@@ -63,7 +64,7 @@ constexpr int kUpdWarp0 = 2 + kPf;                // first updater warp
 constexpr int kExactWarp = kMcThreads / 32 - 1;   // the last warp: exact decisions
 constexpr int kMcUpdaters = kMcThreads - 32 * kUpdWarp0 - 32;
 constexpr int kBarCount = 32 + kMcUpdaters;       // decider + updaters (barriers 1, 2)
-constexpr int kBarExReq = 3, kBarExDone = 4;      // decider + exact warp (64 threads)
+constexpr int kBarExReq = 3;                      // wakes the exact warp (decider + exact warp, 64 threads)
 constexpr int kRing = 256;      // neighbour sites kept per neighbour (power of two)
 constexpr int kLogWords = 32;   // neighbour accept words kept per neighbour (power of two)
 constexpr int kBmBits = 2048;   // bits of a batch's neighbour-site bitmap (hashed sites, power of two)
@@ -140,6 +141,7 @@ struct McShared {
     int nflip;
     // exact decisions (rare): the decider posts a trial, the exact warp answers
     int exX, exBits;       // the trial's site; its FP64 outcomes for qL + qR = -2, 0, +2 (bits 0-2)
+    volatile int exDone;   // number of the latest answer (exact warp; the decider counts its requests)
     float exQ, exU, exG, exBeta;
 };
 
@@ -301,6 +303,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         S.applied[0] = S.applied[1] = 0;
         for (int i = 0; i < kPre; ++i) S.readyTag[i] = 0;
         S.decDone = 0;
+        S.exDone = 0;
         S.done = 0;
         S.nflip = 0;
     }
@@ -321,6 +324,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         for (int t = 0; t < kGv; ++t) gv[t] = 0.f;
 
         int A0 = 0, A1 = 0;  // neighbour iterations applied to the ghost rows
+        int exSeq = 0;       // exact-decision requests posted
 
         // Applies the published neighbour iterations below lim0 / lim1 (their sites
         // are in the ring) to the ghost rows; returns the helper's availability word.
@@ -489,7 +493,8 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                         // fb is flagged: the exact warp decides its trial in FP64 from the
                         // exact field (every flip before the trial is in qs), for each value
                         // of the neighbours' spin sum; then the round is evaluated again.
-                        // (Named barriers: no polling; the exact warp sleeps between requests.)
+                        // (The decider's arrival on a named barrier wakes the exact warp, which
+                        // sleeps there between requests; the decider's wait is bounded.)
                         if (lane == fb) {
                             const int sl = (g0 + lane) / N;
                             S.exX = x;
@@ -498,8 +503,14 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                             S.exG = T.G ? T.G[sl] : T.Gs;
                             S.exBeta = T.beta ? T.beta[sl] : T.betas;
                         }
-                        bar_sync(kBarExReq, 64);
-                        bar_sync(kBarExDone, 64);
+                        ++exSeq;
+                        __syncwarp();
+                        __threadfence_block();
+                        bar_arrive(kBarExReq, 64);
+                        if (!wait_until(waitNs, [&] { return uniform_acquire(&S.exDone) == exSeq; })) {
+                            aborted = true;
+                            break;
+                        }
                         if (lane == fb) {
                             exBits = S.exBits;
                             exValid = true;
@@ -615,7 +626,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         __syncwarp();
         __threadfence_block();
         bar_arrive(1, kBarCount);
-        bar_sync(kBarExReq, 64);  // the exact warp sees done and leaves
+        bar_arrive(kBarExReq, 64);  // the exact warp sees done and leaves
     } else if (warp == 1) {
         // -------------------------------------------------------------- helper
         // lane l < 4 polls word (avail[n] >> 5) + dw of neighbour n = l & 1, dw = l >> 1
@@ -655,11 +666,12 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         }
     } else if (warp == kExactWarp) {
         // --------------------------------------------------------- exact warp
-        // Sleeps on a named barrier until the decider posts a flagged trial: sums
+        // Sleeps on a named barrier until the decider posts a flagged trial (or
+        // the end of the sweep) and arrives on it: sums
         // its exact field (the integer row sum, as the one-CTA kernel computes it)
         // and decides it in FP64 for each value of the neighbours' spin sum (lane
         // k < 3: the sum 2k - 2).
-        for (;;) {
+        for (int seq = 1;; ++seq) {
             bar_sync(kBarExReq, 64);
             if (S.done) break;
             const int xr = S.exX;
@@ -671,10 +683,11 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                                                    m, Gr, br, ur)
                                     : 0;
             const unsigned bits = __ballot_sync(FULL, ok) & 7u;
-            if (lane == 0) S.exBits = (int)bits;
+            if (lane == 0) {
+                S.exBits = (int)bits;
+                st_release_cta(&S.exDone, seq);
+            }
             __syncwarp();
-            __threadfence_block();
-            bar_arrive(kBarExDone, 64);
         }
     } else if (warp < kUpdWarp0) {
         // --------------------------------------------------------- prefetchers

@@ -388,7 +388,7 @@ private:
             size_t N0 = r.N0, N1 = r.N1, m = r.m;
             s += al(N0 * N1 * 4) + al(N0 * 4) + al(N1 * 4) + al(m * N0) + al(m * N1) + al(m * N0 * 4) +
                  al(m * N1 * 4) + al(m * N1 * 8);
-            if (sq103_bipartite_refresh_uses_tc((int)N0, (int)N1))
+            if (sq103_bipartite_refresh_uses_tc((int)N0, (int)N1, (int)m))
                 s += al(sq103_tc_digits_bytes((int)N1, (int)N0)) + al(sq103_tc_digits_bytes((int)N0, (int)N1)) +
                      al(sq103_tc_spins_bytes((int)m, (int)std::max(N0, N1)));
         }
@@ -413,7 +413,7 @@ private:
             const bool large = r->kind == kSearch ? false
                                : r->kind == 0 ? !fitsStaging(*r) && sq103_dense_multicta_ok(r->N0, r->m, kColoring)
                                               : (size_t)r->m * r->N0 * r->N1 > kBipLargeWork ||
-                                                    sq103_bipartite_refresh_uses_tc(r->N0, r->N1);
+                                                    sq103_bipartite_refresh_uses_tc(r->N0, r->N1, r->m);
             const bool fits =
                 used_ + r->bytes <= budget_ &&
                 (r->kind == kSearch ? (int)searches_.size() < kMaxSearches
@@ -514,7 +514,7 @@ private:
             }
         } else {
             const size_t N0 = r->N0, N1 = r->N1;
-            const bool tc = sq103_bipartite_refresh_uses_tc((int)N0, (int)N1);  // as the single-instance annealer
+            const bool tc = sq103_bipartite_refresh_uses_tc((int)N0, (int)N1, m);  // as the single-instance annealer
             size_t oG = 0, oB = al(n * 4), oJ = oB + al(n * 4), oh0 = oJ + al(N0 * N1 * 4), oh1 = oh0 + al(N0 * 4),
                    oc = oh1 + al(N1 * 4), oq0 = oc + 512, oq1 = oq0 + al(m * N0), oF0 = oq1 + al(m * N1),
                    oF1 = oF0 + al(m * N0 * 4), oR = oF1 + al(m * N1 * 4), oE = oR + al(std::max(m * N1, N0 + N1) * 8),

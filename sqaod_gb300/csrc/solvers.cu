@@ -7,8 +7,9 @@
 //   dense BF           sqaodc/cuda/CUDADenseGraphBFSearcher.cpp:15-185
 //   bipartite BF       sqaodc/cuda/CUDABipartiteGraphBFSearcher.cpp
 // with these differences, each deliberate:
-//   - the dense annealer also offers algorithm "naive" (the CPU solver's
-//     menu: naive / coloring / sa_naive), as the target API lists it;
+//   - the naive sweeps (dense naive, bipartite naive and sa_naive) are
+//     kernel-layer entry points; the annealers select algorithms as the
+//     reference's CUDA annealers do (naive runs coloring);
 //   - random numbers come from the in-kernel Philox stream
 //     (seed, step counter), so a seeded run replays bit-exactly;
 //   - returned energies are evaluated in FP64 on the GPU;
@@ -118,12 +119,20 @@ public:
         SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
     }
 
+    // As the reference's CUDA annealer (CUDADenseGraphAnnealer.cu): coloring for
+    // naive, sa_naive for sa_coloring.  The naive sweep kernels stay available at
+    // the kernel layer (sq103_dense_anneal with algo 0).
     sq::Algorithm selectAlgorithm(sq::Algorithm algo) override {
         switch (algo) {
-        case sq::algoNaive:
         case sq::algoColoring:
         case sq::algoSANaive:
             algo_ = algo;
+            break;
+        case sq::algoNaive:
+            algo_ = sq::algoColoring;
+            break;
+        case sq::algoSAColoring:
+            algo_ = sq::algoSANaive;
             break;
         default:
             selectDefaultAlgorithm(algo, sq::algoColoring, sq::algoSANaive);
@@ -647,13 +656,20 @@ public:
         SQ_CHECK(cudaSetDevice(static_cast<DeviceImpl &>(device).devNo_));
     }
 
+    // As the reference's CUDA annealer (CUDABipartiteGraphAnnealer.cu): coloring
+    // for naive, sa_coloring for sa_naive.  The naive and sa_naive kernels stay
+    // available at the kernel layer (sq103_bipartite_anneal with algo 0 / 2).
     sq::Algorithm selectAlgorithm(sq::Algorithm algo) override {
         switch (algo) {
-        case sq::algoNaive:
         case sq::algoColoring:
-        case sq::algoSANaive:
         case sq::algoSAColoring:
             algo_ = algo;
+            break;
+        case sq::algoNaive:
+            algo_ = sq::algoColoring;
+            break;
+        case sq::algoSANaive:
+            algo_ = sq::algoSAColoring;
             break;
         default:
             selectDefaultAlgorithm(algo, sq::algoColoring, sq::algoSAColoring);
@@ -814,7 +830,7 @@ public:
         d_q1_.ensure((size_t)m_ * N1_);
         d_F0_.ensure((size_t)m_ * N0_);
         d_F1_.ensure((size_t)m_ * N1_);
-        if (d_digits1_.p) d_Abf_.ensure(sq103_tc_spins_bytes(m_, std::max(N0_, N1_)));
+        if (useTc()) d_Abf_.ensure(sq103_tc_spins_bytes(m_, std::max(N0_, N1_)));
         d_E64_.ensure(m_);
         h_E64_.ensure(m_);
         h_q0_.ensure((size_t)m_ * N0_);
@@ -989,9 +1005,10 @@ private:
         d_scratch_.ensure(N0_ + N1_);
         d_status_.ensure(1);
         SQ_CHECK(cudaMemsetAsync(d_status_.p, 0, sizeof(int), st_.get()));
-        // large problems compute the half-step fields on the tensor cores from digit
-        // planes of J (for F1) and of J^T (for F0)
-        if (sq103_bipartite_refresh_uses_tc(N0_, N1_)) {
+        // large problems may compute the half-step fields on the tensor cores from
+        // digit planes of J (for F1) and of J^T (for F0): made with the problem, used
+        // when the trotter count also allows (sq103_bipartite_refresh_uses_tc)
+        if ((long long)N0_ * N1_ >= (1ll << 20)) {
             d_digits1_.ensure(sq103_tc_digits_bytes(N1_, N0_));
             d_digits0_.ensure(sq103_tc_digits_bytes(N0_, N1_));
         } else {
@@ -999,6 +1016,8 @@ private:
             d_digits0_.release();
         }
     }
+
+    bool useTc() const { return d_digits1_.p && sq103_bipartite_refresh_uses_tc(N0_, N1_, m_); }
 
     void makeDigits() {
         if (!d_digits1_.p) return;
@@ -1077,9 +1096,10 @@ private:
         t.J64 = fp64_ ? d_J64_.p : nullptr;
         t.h0_64 = fp64_ ? d_h0_64_.p : nullptr;
         t.h1_64 = fp64_ ? d_h1_64_.p : nullptr;
-        t.digits1 = d_digits1_.p;
-        t.digits0 = d_digits0_.p;
-        t.spinsBf16 = d_Abf_.p;
+        const bool tc = useTc();
+        t.digits1 = tc ? d_digits1_.p : nullptr;
+        t.digits0 = tc ? d_digits0_.p : nullptr;
+        t.spinsBf16 = tc ? d_Abf_.p : nullptr;
         t.status = d_status_.p;
         SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
         step_ += (uint32_t)nSteps;

@@ -36,6 +36,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -431,9 +432,14 @@ SQ103_API int sq103_tc_refresh(const void *digits, int R, int K, const int8_t *q
 // so every path that anneals the same instance holds the same fields.
 SQ103_API int sq103_dense_refresh_uses_tc(int N) { return N >= 1024 ? 1 : 0; }
 
-// bipartite half-step fields on the tensor cores for problems of at least 2^20 couplings
-SQ103_API int sq103_bipartite_refresh_uses_tc(int N0, int N1) {
-    return (long long)N0 * (long long)N1 >= (1ll << 20) ? 1 : 0;
+// Bipartite half-step fields on the tensor cores for problems of at least 2^20
+// couplings whose output tiles (128 trotters x 64 spins) give each half step a
+// grid of at least 64 CTAs; smaller grids leave most SMs idle, and the SIMT
+// field kernel is faster there (N0 = N1 = 1024, m = 64: 16 CTAs).
+SQ103_API int sq103_bipartite_refresh_uses_tc(int N0, int N1, int m) {
+    if ((long long)N0 * (long long)N1 < (1ll << 20) || m < 1) return 0;
+    const long long tiles = (long long)((m + 127) / 128) * ((std::min(N0, N1) + 63) / 64);
+    return tiles >= 64 ? 1 : 0;
 }
 
 SQ103_API int sq103_dense_refresh(const float *J, int ldJ, const void *digits, void *spinsBf16, const int8_t *q,

@@ -174,8 +174,8 @@ class DenseGraphAnnealer(_Handle):
         return self._bits('get_q')
 
     def set_q(self, q):
-        q = common.fix_type(np.asarray(q), np.int8)
-        self._call('set_q', ptr(q), _c_int(q.shape[-1]))
+        q = np.ascontiguousarray(common.fix_type(np.asarray(q), np.int8)).ravel()
+        self._call('set_q', ptr(q), _c_int(len(q)))
 
     def set_qset(self, qset):
         qs = np.ascontiguousarray(np.array([common.fix_type(np.asarray(v), np.int8) for v in qset]), np.int8)
@@ -346,7 +346,8 @@ class BipartiteGraphAnnealer(_Handle):
         return self._pairs('get_q')
 
     def set_q(self, qpair):
-        q0, q1 = (common.fix_type(np.asarray(v), np.int8) for v in qpair)
+        # any shape with N0 (N1) elements, e.g. the (1, N) rows of bit_to_spin, as the reference takes them
+        q0, q1 = (np.ascontiguousarray(common.fix_type(np.asarray(v), np.int8)).ravel() for v in qpair)
         self._call('set_q', ptr(q0), ptr(q1), _c_int(len(q0)), _c_int(len(q1)))
 
     def set_qset(self, qset):

@@ -55,9 +55,10 @@ def test_annealer_preferences_on_host():
     a = sq.cuda.dense_graph_annealer()
     p = a.get_preferences()
     assert p["algorithm"] == "coloring" and p["precision"] == "float" and p["device"] == "cuda"
+    # as the reference's CUDA annealers (sqaodpy/tests/test_dense_graph_annealer.py:453-471)
     a.set_preferences(algorithm=sq.algorithm.naive, n_trotters=7)
     p = a.get_preferences()
-    assert p["algorithm"] == "naive" and p["n_trotters"] == 7
+    assert p["algorithm"] == "coloring" and p["n_trotters"] == 7
     a.set_preferences(algorithm=sq.algorithm.sa_default)
     assert a.get_preferences()["algorithm"] == "sa_naive"
     a.set_preferences(algorithm=sq.algorithm.sa_coloring)
@@ -68,7 +69,9 @@ def test_annealer_preferences_on_host():
     b.set_preferences(algorithm=sq.algorithm.sa_default)
     assert b.get_preferences()["algorithm"] == "sa_coloring"
     b.set_preferences(algorithm=sq.algorithm.naive)
-    assert b.get_preferences()["algorithm"] == "naive"
+    assert b.get_preferences()["algorithm"] == "coloring"
+    b.set_preferences(algorithm=sq.algorithm.sa_naive)
+    assert b.get_preferences()["algorithm"] == "sa_coloring"
 
 
 def test_searcher_preferences_on_host():

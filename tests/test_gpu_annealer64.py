@@ -34,7 +34,7 @@ def _sym64(rng, N):
 
 @pytest.mark.parametrize("N,m,algo,opt", [(96, 8, "coloring", "min"), (130, 5, "coloring", "max"),
                                           (1100, 16, "coloring", "min"), (64, 6, "sa_naive", "min"),
-                                          (48, 4, "naive", "min")])
+                                          (48, 4, "coloring", "max")])
 def test_dense_annealer64_replays_fp64(sq, orc, N, m, algo, opt):
     rng = np.random.default_rng(N + m)
     W = _sym64(rng, N)
