@@ -590,7 +590,7 @@ SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int
                                   long long capBytes, int release);
 SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *done,
                                  unsigned long long *bytesInUse);
-/* at most n large instances admitted at a time (default 8; dense: one CTA per
+/* at most n large instances admitted at a time (default 32; dense: one CTA per
  * trotter, packed up to 8 per launch; bipartite: per-instance kernels) */
 SQ103_API int sq103_server_set_large_limit(void *handle, int n);
 /* Fault injection from the host (tests; no counterpart in the reference): writes

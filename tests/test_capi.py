@@ -186,3 +186,14 @@ void use() {
     r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", inc, "-c", str(src), "-o", str(tmp_path / "caller.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_factory_default_dtypes_on_host():
+    """The sqaod_gb300.cuda factories default to float32 (the benchmark
+    precision); the reference's default float64 is one argument away."""
+    import numpy as np
+    import sqaod_gb300 as sq
+    for make in (sq.cuda.dense_graph_annealer, sq.cuda.bipartite_graph_annealer, sq.cuda.dense_graph_bf_searcher,
+                 sq.cuda.bipartite_graph_bf_searcher):
+        assert make().dtype is np.float32
+        assert make(dtype=np.float64).dtype is np.float64
