@@ -53,6 +53,8 @@
 #include <algorithm>
 #include <mutex>
 
+// the exact warp's helpers inlined: measured 1.8 % faster at N=4096 m=256
+#define SQ103_EXACT_ATTR __forceinline__
 #include "sq_common.cuh"
 #include "sq_kernels.h"
 

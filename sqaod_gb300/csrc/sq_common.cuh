@@ -217,9 +217,18 @@ __device__ __forceinline__ double exact_value(long long s, int S) {
     return __dmul_rn(__ll2double_rn(s), __longlong_as_double((long long)(1023 - S) << 52));
 }
 
+// The exact-decision helpers are kept out of line by default (they are rare,
+// and inlined copies grow every kernel's hot code); a file may define
+// SQ103_EXACT_ATTR as __forceinline__ before including this header when that
+// measures faster (the one-CTA-per-trotter sweep, which calls them from a warp
+// of their own).
+#ifndef SQ103_EXACT_ATTR
+#define SQ103_EXACT_ATTR __noinline__
+#endif
+
 // one thread; the couplings are Jx[j * stride] (a row of J, or a column with stride = ld)
 template <class R>
-static __device__ __noinline__ double exact_field_thread(const R *Jx, size_t stride, const int8_t *q, int N) {
+static __device__ SQ103_EXACT_ATTR double exact_field_thread(const R *Jx, size_t stride, const int8_t *q, int N) {
     unsigned e = 0;
     for (int j = 0; j < N; ++j) e = max(e, ExactFx<R>::expo(Jx[j * stride]));
     const int S = ExactFx<R>::shift(e, log2_ceil(N));
@@ -233,7 +242,7 @@ static __device__ __noinline__ double exact_field_thread(const R *Jx, size_t str
 
 // warp-wide: every lane of the (converged) warp calls it and gets the sum
 template <class R>
-static __device__ __noinline__ double exact_field_warp(const R *Jx, const int8_t *q, int N) {
+static __device__ SQ103_EXACT_ATTR double exact_field_warp(const R *Jx, const int8_t *q, int N) {
     const int lane = threadIdx.x & 31;
     unsigned e = 0;
     for (int j = lane; j < N; j += 32) e = max(e, ExactFx<R>::expo(Jx[j]));
@@ -253,7 +262,7 @@ static __device__ __noinline__ double exact_field_warp(const R *Jx, const int8_t
 // per lane (the row of N = 4096 in four rounds); the second pass finds the row
 // in L1.  The same integer sum as the generic form.
 template <>
-__device__ __noinline__ double exact_field_warp<float>(const float *Jx, const int8_t *q, int N) {
+__device__ SQ103_EXACT_ATTR double exact_field_warp<float>(const float *Jx, const int8_t *q, int N) {
     typedef ExactFx<float> X;
     const int lane = threadIdx.x & 31;
     const bool vec = (reinterpret_cast<uintptr_t>(Jx) & 15) == 0 && (reinterpret_cast<uintptr_t>(q) & 3) == 0;
@@ -317,7 +326,7 @@ __device__ __forceinline__ int exact_accept_coef(bool sa, bool twoF, float q, do
 // coef = log(tanh(G beta / m)) / beta, rate beta; SA dE = 2 q (h + 2F), rate 1/G;
 // accept iff dE < 0 or exp(-dE rate) > u.  For bipartite trials (dE with h + F)
 // pass twoF = false.
-static __device__ __noinline__ int exact_accept(bool sa, bool twoF, float q, double h, double F, float qL, float qR,
+static __device__ SQ103_EXACT_ATTR int exact_accept(bool sa, bool twoF, float q, double h, double F, float qL, float qR,
                                                 int m, float G, float beta, float u) {
     const double coef = sa ? 0.0 : exact_ring_coef(G, beta, m);
     return exact_accept_coef(sa, twoF, q, h, F, (int)qL + (int)qR, m, G, beta, coef, u);
