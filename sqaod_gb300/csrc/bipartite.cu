@@ -105,6 +105,54 @@ __global__ void __launch_bounds__(256) bip_flip_phase(int8_t *qA, const float *F
     }
 }
 
+// All colour phases of one SQA half-step in one launch.  A trial's neighbours
+// are the same spin index in the adjacent trotters, so a block that owns whole
+// columns (spin i of every trotter) orders the phases with __syncthreads:
+// even trotters, then trotter m-1 when m is odd, then odd trotters.  Thread t
+// of a block takes column i0 + t % C and trotter pairs t / C, t / C + 256 / C,
+// ... (C columns per block, chosen so the pairs of a column fill the block);
+// the trials, their draws and their arithmetic are those of bip_flip_phase, so
+// the spins, trace and accepted count are identical, with one launch per
+// half-step in place of two or three.
+__global__ void __launch_bounds__(256) bip_flip_half(int8_t *qA, const float *F, const float *h, int Ns, int m, int C,
+                                                     uint64_t seed, uint32_t step, uint32_t tag, const float *Gp,
+                                                     const float *bp, float Gsc, float bsc, int algo, uint32_t *trace,
+                                                     unsigned long long bitBase, unsigned long long *accepted,
+                                                     BipFixed B) {
+    const int t = (int)threadIdx.x;
+    const int i = (int)blockIdx.x * C + t % C, p0 = t / C, pStride = (int)blockDim.x / C;
+    const bool col = t < pStride * C && i < Ns;
+    const float G = Gp ? *Gp : Gsc, beta = bp ? *bp : bsc;
+    const StepConst sc = step_const(algo, m, G, beta);
+    B.G = G;
+    B.beta = beta;
+    const int pairs = m / 2;
+    unsigned long long acc = 0;
+    for (int ph = 0; ph < 3; ++ph) {
+        if (ph == 1 && !(m & 1)) continue;
+        if (col) {
+            if (ph == 1) {
+                if (p0 == 0) acc += bip_trial(qA, F, h, Ns, m, m - 1, i, seed, step, tag, sc, algo, trace, bitBase, B);
+            } else {
+                for (int p = p0; p < pairs; p += pStride)
+                    acc += bip_trial(qA, F, h, Ns, m, 2 * p + (ph == 2 ? 1 : 0), i, seed, step, tag, sc, algo, trace,
+                                     bitBase, B);
+            }
+        }
+        __syncthreads();
+    }
+    if (accepted) {
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0 && acc) atomicAdd(accepted, acc);
+    }
+}
+
+// columns per block of bip_flip_half: the trotter pairs of a column fill the block
+static int flip_half_cols(int m) {
+    const int pairs = std::max(1, m / 2);
+    return pairs >= 256 ? 1 : 256 / pairs;
+}
+
 // fixed-order block sum (256 threads) in fp32
 __device__ float block_sum_f32(float v, float *red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -330,6 +378,18 @@ extern "C" SQ103_API int sq103_bipartite_anneal(const sq103_bipartite_task *task
                 sq103_bipartite_fields(T.J, T.N0, T.N1, side ? T.q0 : T.q1, side, F, m, stream);
             }
             const uint32_t tag = (uint32_t)(sa ? kTagBipSA : kTagBipSweep) | ((uint32_t)side << 8);
+            const BipFixed fixedSide{T.J, T.N0, side ? T.q0 : T.q1, side ? T.N0 : T.N1, side, 0.f, 0.f, T.J64,
+                                     side ? T.h1_64 : T.h0_64};
+            if (!sa) {
+                // every colour phase of the half-step in one launch (blocks own whole columns)
+                const int C = flip_half_cols(m);
+                bip_flip_half<<<(Ns + C - 1) / C, 256, 0, st>>>(qA, F, h, Ns, m, C, T.seed, step, tag,
+                                                               T.G ? T.G + s : nullptr, T.beta ? T.beta + s : nullptr,
+                                                               T.Gs, T.betas, T.algo, trace, bitBase, T.accepted,
+                                                               fixedSide);
+                bitBase += (unsigned long long)m * Ns;
+                continue;
+            }
             for (int ph = 0; ph < 3; ++ph) {
                 int yb, ys, cnt;
                 if (sa) {
