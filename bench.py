@@ -469,6 +469,12 @@ def run_batched(args, world):
     torch.cuda.synchronize()
     t_add = time.perf_counter() - t_add
     t_tune = time.perf_counter()
+    # trotters per CTA: the one-CTA-per-trotter size limit (default 1024, from whole-run measurements;
+    # --autotune-routing times 8 steps per candidate instead); then the staging size, by measurement
+    if args.autotune_routing and args.multicta_min_n is None:
+        routing = b.autotune_routing(8)
+    else:
+        routing = 1024 if args.multicta_min_n is None else args.multicta_min_n
     smem = b.autotune(2)
     b.anneal(1, use_graph=True)  # capture + warm up
     b.sync()
@@ -513,7 +519,10 @@ def run_batched(args, world):
             "data": "synthetic (W uniform[-1,1] symmetric, seed 1000 + i)",
             "config": {"workload": "1024 dense instances, N log-uniform [64, 2048], m in {8..128}, coloring, "
                                    "beta=50, %d steps of G=5*0.99^k" % steps, "smem_per_cta": smem,
-                       "multicta_min_n": 1024 if args.multicta_min_n is None else args.multicta_min_n,
+                       "multicta_min_n": routing,
+                       "routing": ("autotuned (8 trial steps per candidate 0, 512, 768, 1024, 1400, 2048)"
+                                   if args.autotune_routing and args.multicta_min_n is None
+                                   else "given" if args.multicta_min_n is not None else "default"),
                        "multicta_instances": b.multicta_count()},
             "batched": {"seconds": t_batch, "solves_per_s": len(work) / t_batch, "setup_s": t_add,
                         "results_s": t_out, "seconds_with_setup": t_total,
@@ -835,6 +844,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")
     ap.add_argument("--plain-sample", type=int, default=0,
                     help="batched mode: instances solved on the plain path (0: all of them)")
+    ap.add_argument("--autotune-routing", action="store_true",
+                    help="batched mode: choose the one-CTA-per-trotter size limit by timing 8 steps per candidate")
     ap.add_argument("--multicta-min-n", type=int, default=None,
                     help="batched mode: instances of at least this N take the one-CTA-per-trotter sweep (default 1024)")
     ap.add_argument("--cpu-leg", action="store_true", help="internal: time the CPU reference annealer alone")

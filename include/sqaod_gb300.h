@@ -482,6 +482,13 @@ SQ103_API int sq103_dense_batch_set_multicta_min_n(void *handle, int N);
 /* instances on the one-CTA-per-trotter sweep since the last prepare */
 SQ103_API int sq103_dense_batch_multicta_count(void *handle, int *n);
 SQ103_API int sq103_dense_batch_autotune(void *handle, int trialSteps, int *smemBytes);
+/* Trotters per CTA by measurement (no counterpart in the reference): prepares the
+ * batch with each candidate size limit of sq103_dense_batch_set_multicta_min_n
+ * (one CTA per trotter at or above it, one CTA per instance below), times
+ * trialSteps steps from the start of the schedule, keeps the fastest and prepares
+ * again (the state is that of a fresh prepare, whatever the choice). */
+SQ103_API int sq103_dense_batch_autotune_routing(void *handle, int trialSteps, const int *candidates, int n,
+                                                int *chosen);
 SQ103_API int sq103_dense_batch_anneal(void *handle, int nSteps, int useGraph);
 SQ103_API int sq103_dense_batch_sync(void *handle);
 SQ103_API int sq103_dense_batch_info(void *handle, int *nInst, int *pos, int *grid, int *smemBytes);

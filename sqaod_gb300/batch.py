@@ -67,6 +67,17 @@ class DenseBatchAnnealer:
         self._call("multicta_count", ctypes.byref(n))
         return n.value
 
+    def autotune_routing(self, trial_steps=8, candidates=(0, 512, 768, 1024, 1400, 2048)):
+        """Chooses, by timing trial_steps steps from the start of the schedule,
+        the size limit at and above which instances take one CTA per trotter
+        (set_multicta_min_n); prepares the batch again with it and returns it.
+        The results do not depend on the choice."""
+        c = np.ascontiguousarray(candidates, np.int32)
+        chosen = ctypes.c_int()
+        self._call("autotune_routing", ctypes.c_int(int(trial_steps)), ptr(c), ctypes.c_int(len(c)),
+                   ctypes.byref(chosen))
+        return chosen.value
+
     def autotune(self, trial_steps=2):
         s = ctypes.c_int()
         self._call("autotune", ctypes.c_int(trial_steps), ctypes.byref(s))

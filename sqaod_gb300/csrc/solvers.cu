@@ -2034,6 +2034,43 @@ public:
     }
 
     // times a few candidate configurations on copies of the instance state and keeps the fastest
+    // Trotters per CTA, by measurement: for each candidate size limit (instances of
+    // at least that many spins take one CTA per trotter in packed launches, the
+    // rest one CTA per instance in the persistent kernel; 0: every instance in the
+    // persistent kernel) the batch is prepared and `trialSteps` steps from the start
+    // of the schedule are timed; the fastest limit is kept and the batch prepared
+    // again, so the results do not depend on the choice.  Returns the limit.
+    int autotuneRouting(int trialSteps, const int *cands, int nCands) {
+        throwErrorIf(!cands || nCands < 1, "no candidate size limit.");
+        throwErrorIf(insts_.empty() || nSched_ <= 0, "add instances and set a schedule first.");
+        const int steps = std::max(1, std::min(trialSteps, nSched_));
+        cudaEvent_t e0, e1;
+        SQ_CHECK(cudaEventCreate(&e0));
+        SQ_CHECK(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int bestN = multiMinN_;
+        for (int i = 0; i < nCands; ++i) {
+            throwErrorIf(cands[i] < 0, "size limits must not be negative.");
+            multiMinN_ = cands[i];
+            prepare();
+            SQ_CHECK(cudaEventRecord(e0, st_.get()));
+            anneal(steps, true);
+            SQ_CHECK(cudaEventRecord(e1, st_.get()));
+            sync();
+            float ms = 0.f;
+            SQ_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bestN = cands[i];
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        multiMinN_ = bestN;
+        prepare();
+        return bestN;
+    }
+
     int autotune(int trialSteps) {
         throwErrorIf(!prepared_, "prepare() first.");
         const int n = (int)insts_.size();

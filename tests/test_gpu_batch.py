@@ -61,3 +61,33 @@ def test_batch_equals_single(use_graph, min_n):
         a.anneal(G, 30.0)
         assert np.array_equal(np.array(a.get_q()), b.get_q(i)), i
         assert np.array_equal(a.get_E64(), b.get_E64(i)), i
+
+
+def test_batch_routing_autotune_keeps_results():
+    """autotune_routing times each candidate size limit from a fresh prepare and
+    prepares again with the fastest: it returns one of the candidates, the
+    packed-instance count follows it, and every instance still ends as alone."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.batch import DenseBatchAnnealer
+    probs = _problems(10, seed=3)
+    G = _schedule(12)
+    b = DenseBatchAnnealer()
+    for W, m, seed in probs:
+        b.add(W, m, sq.minimize, seed)
+    b.set_schedule(G, 30.0)
+    b.prepare()
+    cands = (0, 256, 1024)
+    chosen = b.autotune_routing(4, cands)
+    assert chosen in cands
+    expect = sum(1 for W, m, _ in probs if chosen > 0 and W.shape[0] >= chosen and m >= 2)
+    assert b.multicta_count() == expect
+    assert b.info()["position"] == 0
+    b.anneal(len(G))
+    for i, (W, m, seed) in enumerate(probs):
+        a = sq.cuda.dense_graph_annealer(W, n_trotters=m, algorithm="sa_naive" if m == 1 else "coloring")
+        a.seed(seed)
+        a.prepare()
+        a.randomize_spin()
+        a.anneal(G, 30.0)
+        assert np.array_equal(np.array(a.get_q()), b.get_q(i)), i
+        assert np.array_equal(a.get_E64(), b.get_E64(i)), i
