@@ -150,6 +150,43 @@ def test_c2_bipartite_replays_fp64(sq, orc, algo, start):
     assert tot["n_mismatch"] == tot["n_mismatch_small"], tot
 
 
+def test_bipartite_tensor_core_fields_replay_fp64(sq, orc):
+    """A bipartite annealer whose half-step fields come from the tensor cores
+    (N0 = N1 = 2048, m = 256: 64 output tiles per half step), replayed against
+    FP64 over two steps."""
+    from sqaod_gb300 import _lib
+    N0 = N1 = 2048
+    m = 256
+    assert _lib.lib().sq103_bipartite_refresh_uses_tc(N0, N1, m) == 1
+    rs = np.random.RandomState(5)
+    b0 = rs.uniform(-1, 1, N0).astype(np.float32)
+    b1 = rs.uniform(-1, 1, N1).astype(np.float32)
+    W = rs.uniform(-1, 1, (N1, N0)).astype(np.float32)
+    a = sq.cuda.bipartite_graph_annealer(b0, b1, W, n_trotters=m, algorithm="coloring")
+    seed = 11
+    a.seed(seed)
+    a.prepare()
+    a.randomize_spin()
+    pairs = a.get_q()
+    q0 = np.array([p[0] for p in pairs])
+    q1 = np.array([p[1] for p in pairs])
+    h0, h1, J, c = a.get_hamiltonian()
+    a.set_trace(True)
+    tot = {}
+    for G in (2.0, 0.05):
+        _, step = a.get_rng_state()
+        a.anneal_one_step(G, BETA)
+        trace = a.get_trace((m * (N0 + N1) + 31) // 32)
+        q0, q1, st = orc.bg_replay(h0, h1, J, m, orc.ALGO_COLORING, seed, step, G, BETA, q0, q1, trace, MARGIN_TOL)
+        pairs = a.get_q()
+        assert np.array_equal(np.array([p[0] for p in pairs]), q0)
+        assert np.array_equal(np.array([p[1] for p in pairs]), q1)
+        for k, v in st.items():
+            tot[k] = max(tot.get(k, 0), v) if k == "max_mismatch_margin" else tot.get(k, 0) + v
+    print("bipartite on tensor-core fields: %s" % tot)
+    assert tot["n_mismatch"] == tot["n_mismatch_small"], tot
+
+
 @pytest.mark.parametrize("optimize", ["minimize", "maximize"])
 def test_c3_bf_n32_exact(sq, orc, optimize):
     """All 2^32 states of the bench's N = 32 integer QUBO: Emin and every
