@@ -838,7 +838,7 @@ def main():
     ap.add_argument("--plain-per-stratum", type=int, default=3,
                     help="served mode: plain solves timed per stratum of the stream (16 strata)")
     ap.add_argument("--slots", type=int, default=512, help="served mode: concurrent instances per kind")
-    ap.add_argument("--large", type=int, default=32,
+    ap.add_argument("--large", type=int, default=64,
                     help="served mode: concurrent large instances (dense ones step together in packed launches)")
     ap.add_argument("--check", type=int, default=16, help="served mode: requests compared with the plain path")
     ap.add_argument("--batch-steps", type=int, default=0, help="batched mode: steps (0 = the whole schedule)")

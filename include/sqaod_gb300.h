@@ -101,7 +101,7 @@ SQ103_API unsigned long long sq103_dense_ws_bytes(int N, int m, int nSteps);
 /* 1 if the one-CTA-per-trotter sweep can run this shape on the current device (N >= 64, m >= 2;
  * the launch also needs ldJ % 4 == 0 and a 16-byte aligned J) */
 SQ103_API int sq103_dense_multicta_ok(int N, int m, int algo);
-/* No counterpart in the reference.  Up to 8 independent instances in one
+/* No counterpart in the reference.  Up to 16 independent instances in one
  * cooperative launch of the one-CTA-per-trotter sweep (their trotter counts
  * summed within sq103_dense_multicta_capacity of the largest N); each task
  * needs its own ws.  Every instance ends exactly as when launched alone. */
@@ -597,8 +597,8 @@ SQ103_API int sq103_server_result(void *handle, int id, double *E, int capE, int
                                   long long capBytes, int release);
 SQ103_API int sq103_server_stats(void *handle, int *queued, int *active, int *done,
                                  unsigned long long *bytesInUse);
-/* at most n large instances admitted at a time (default 32; dense: one CTA per
- * trotter, packed up to 8 per launch; bipartite: per-instance kernels) */
+/* at most n large instances admitted at a time (default 64; dense: one CTA per
+ * trotter, packed up to 16 per launch; bipartite: per-instance kernels) */
 SQ103_API int sq103_server_set_large_limit(void *handle, int n);
 /* Fault injection from the host (tests; no counterpart in the reference): writes
  * `value` into the status word of active dense request `id`, in stream order, as a

@@ -211,7 +211,7 @@ __device__ __forceinline__ void window_bits(int x, int Ji, int j0, int pLast, in
 // [base[i], base[i+1]) are the trotters of task t[i], whose accept words live in
 // outLog[i] (nWords[i] per trotter).  Instances do not interact (the prologue's
 // grid sync is the only common step), so each runs exactly as alone.
-constexpr int kMaxPack = 8;
+constexpr int kMaxPack = 16;
 struct McPack {
     sq103_dense_task t[kMaxPack];
     unsigned long long *outLog[kMaxPack];
@@ -245,11 +245,13 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
         break;
             SQ103_PICK(0) SQ103_PICK(1) SQ103_PICK(2) SQ103_PICK(3)
             SQ103_PICK(4) SQ103_PICK(5) SQ103_PICK(6) SQ103_PICK(7)
+            SQ103_PICK(8) SQ103_PICK(9) SQ103_PICK(10) SQ103_PICK(11)
+            SQ103_PICK(12) SQ103_PICK(13) SQ103_PICK(14) SQ103_PICK(15)
 #undef SQ103_PICK
         }
     }
     __syncthreads();
-    static_assert(kMaxPack == 8, "one case per pack entry");
+    static_assert(kMaxPack == 16, "one case per pack entry");
     const sq103_dense_task &T = task;
     unsigned long long *const outLog = sLog;
     const int nWords = sWords;

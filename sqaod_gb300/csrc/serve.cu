@@ -687,7 +687,7 @@ private:
     Stream st_, res_;  // work; result copies
     PinnedStage stage_;
     unsigned long long budget_, used_ = 0;
-    int maxSlots_, maxLarge_ = 32, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
+    int maxSlots_, maxLarge_ = 64, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
     long long ticks_ = 0;
     int hostCount_[2] = {0, 0};
     std::map<int, std::unique_ptr<Request>> all_;
@@ -700,7 +700,7 @@ private:
     DevBuf<sq103_bipartite_task> bTasks_;
     DevBuf<int> dPos_, bPos_, counts_, queues_;
     DevBuf<float> dW_;
-    static constexpr int kMaxPack = 8;  // instances per packed launch (sq103_dense_anneal_pack)
+    static constexpr int kMaxPack = 16;  // instances per packed launch (sq103_dense_anneal_pack)
 };
 
 }  // namespace sq103

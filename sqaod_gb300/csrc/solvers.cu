@@ -1860,7 +1860,7 @@ private:
 class DenseBatch : public sq::NullBase {
 public:
     static constexpr int kRefreshPeriod = 8;
-    static constexpr int kPackMax = 8;           // instances per packed launch
+    static constexpr int kPackMax = 8;           // instances per packed launch (16 measured slower on C4)
     static constexpr int kDefaultMultiMinN = 1024;
 
     // Instances of at least multiMinN_ spins (with m >= 2 that fit the device) run

@@ -129,7 +129,7 @@ class AnnealServer:
         return {"queued": v[0].value, "active": v[1].value, "done": v[2].value, "bytes_in_use": b.value}
 
     def set_large_limit(self, n):
-        """At most n large instances admitted at a time (default 32): dense ones on the
+        """At most n large instances admitted at a time (default 64): dense ones on the
         one-CTA-per-trotter path (packed launches), bipartite ones on the per-instance kernels."""
         self._call("set_large_limit", ctypes.c_int(int(n)))
 

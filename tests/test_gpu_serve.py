@@ -119,6 +119,31 @@ def test_server_packs_large_dense_requests():
         assert np.array_equal(q, np.array(q1)), i
 
 
+def test_server_packs_more_than_eight_requests():
+    """Twelve large small-m dense requests fit one packed cooperative launch
+    (up to 16 instances per launch); each still ends bit-identical to annealing
+    it alone."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    specs = [("d", 900 + 8 * k, 24, 10 + k % 3, "min") for k in range(12)]
+    rng = np.random.default_rng(29)
+    data = [_sym(rng, sp[1]) for sp in specs]
+    srv = AnnealServer(budget_bytes=1 << 30, max_slots=4)
+    srv.set_large_limit(16)
+    ids = []
+    for i, (spec, d) in enumerate(zip(specs, data)):
+        G, beta = _schedule(spec[3])
+        ids.append(srv.submit_dense(d, spec[2], G, beta, sq.minimize, seed=2500 + i))
+    srv.tick()
+    assert srv.stats()["active"] == 12  # all admitted together: one pack of twelve
+    assert srv.run(max_ticks=100) < 100
+    for i, (spec, d, rid) in enumerate(zip(specs, data, ids)):
+        E, q = srv.result(rid)
+        E1, q1 = _alone(sq, spec, d, 2500 + i)
+        assert np.array_equal(E, E1), (i, E, E1)
+        assert np.array_equal(q, np.array(q1)), i
+
+
 def test_server_rejects_oversized_request():
     import sqaod_gb300 as sq
     from sqaod_gb300._lib import SqaodError
