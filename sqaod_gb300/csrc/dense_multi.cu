@@ -51,6 +51,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <array>
 #include <mutex>
 
 // the exact warp's helpers inlined: measured 1.8 % faster at N=4096 m=256
@@ -84,6 +85,7 @@ constexpr unsigned long long kShortWaitNs = 1000000ull;  // task flag kFlagShort
 // SM's shared load/store path to the decider
 constexpr int kPrefetchSleepNs = 128;
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int kSmallN = 512;  // rows up to this many spins take the kSmall instance
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
     unsigned long long v;
@@ -222,7 +224,13 @@ struct McPack {
 
 // kHooks: the test hooks of the task flags are compiled in (short waits, a
 // trotter that withholds its accept words); the production instance has none.
-template <bool kHooks>
+// kSmall: rows of at most kSmallN spins, where the neighbours' sites hit a lane's
+// site often: each prefetcher finds a lane's neighbour candidates by scanning the
+// 96 iterations of batches p - 2 .. p, with the sites of p - 1 and p - 2 drawn
+// again from the neighbours' Philox streams, instead of a ballot per hit over
+// the hashed-site bitmaps of the other prefetcher's batches (which makes the
+// prefetchers wait for each other).  Both give the same candidates.
+template <bool kHooks, bool kSmall>
 __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ McShared S;
@@ -789,10 +797,55 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                 }
                 // batch p - 1 (the other prefetcher's) must be in the ring; its buffer
                 // slot may already hold a later batch (batch p - 2 is this warp's own)
-                if (p > 0 && !wait_until<kPrefetchSleepNs>(waitNs, [&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
+                if (!kSmall && p > 0 &&
+                    !wait_until<kPrefetchSleepNs>(waitNs, [&] { return uniform_acquire(&S.readyTag[(p - 1) & (kPre - 1)]) >= p; }))
                     break;
                 __syncwarp();
                 const int hb = x & (kBmBits - 1);
+                if (kSmall) {
+                    // the sites of the neighbours' iterations 32 (p - q) + lane, q = 1, 2,
+                    // drawn again (the ring's entries for them are the other prefetcher's)
+                    int sites[2][3];
+#pragma unroll
+                    for (int nn = 0; nn < 2; ++nn) {
+                        sites[nn][0] = nn ? cur1 : cur0;
+#pragma unroll
+                        for (int q = 1; q < 3; ++q) {
+                            const int jq = 32 * (p - q) + lane;
+                            int sq = -1;
+                            if (nn < nNbr && jq >= 0) {
+                                const int s2 = jq / N, k2 = jq - s2 * N;
+                                sq = draw_index(draw(T.seed, (uint32_t)k2, (uint32_t)(nn ? nbr1 : nbr0),
+                                                     T.step0 + (uint32_t)s2, tag).x, N);
+                            }
+                            sites[nn][q] = sq;
+                        }
+                    }
+#pragma unroll
+                    for (int nn = 0; nn < 2; ++nn) {
+                        if (nn >= nNbr) break;
+                        const int lim = lane - 1 + (nn ? before1 : before0);
+                        int c0 = -1, c1 = -1, cnt = 0;
+                        // latest first: batch p, then p - 1, then p - 2, each from its last iteration
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            for (int t = 31; t >= 0; --t) {
+                                const int st = __shfl_sync(FULL, sites[nn][q], t);
+                                if (valid && st == x && (q > 0 || t <= lim)) {
+                                    ++cnt;
+                                    const int jj = 32 * (p - q) + t;
+                                    if (c0 < 0)
+                                        c0 = jj;
+                                    else if (c1 < 0)
+                                        c1 = jj;
+                                }
+                            }
+                        }
+                        if (cnt > kCand) c0 = -2;
+                        cand[((buf * 2 + nn) * kCand) * 32 + lane] = c0;
+                        cand[((buf * 2 + nn) * kCand + 1) * 32 + lane] = cnt > kCand ? -1 : c1;
+                    }
+                } else {
 #pragma unroll
                 for (int nn = 0; nn < 2; ++nn) {
                     if (nn >= nNbr) break;
@@ -835,6 +888,7 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                     }
                     cand[((buf * 2 + nn) * kCand) * 32 + lane] = c0;
                     cand[((buf * 2 + nn) * kCand + 1) * 32 + lane] = c1;
+                }
                 }
             }
             float *jg = Jg + buf * kJgStride + lane * 33;
@@ -935,6 +989,11 @@ static size_t multi_smem_bytes(int N) {
            32 * 8 + (size_t)N + 16;
 }
 
+static std::array<const void *, 4> multi_kernels() {
+    return {(const void *)dense_sweep_multi<false, false>, (const void *)dense_sweep_multi<true, false>,
+            (const void *)dense_sweep_multi<false, true>, (const void *)dense_sweep_multi<true, true>};
+}
+
 static int multi_capacity(int N) {
     // the last answer is cached; callers on several host threads share it
     static std::mutex mu;
@@ -947,23 +1006,19 @@ static int multi_capacity(int N) {
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     size_t smem = multi_smem_bytes(N);
     cudaFuncAttributes fa;
-    cudaFuncGetAttributes(&fa, dense_sweep_multi<false>);
+    cudaFuncGetAttributes(&fa, dense_sweep_multi<false, false>);
     if (smem + fa.sharedSizeBytes > (size_t)optin) return 0;
-    for (const void *k : {(const void *)dense_sweep_multi<false>, (const void *)dense_sweep_multi<true>})
-        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    // every instance: the launch takes the one the tasks' flags and sizes ask for
+    perSm = 1 << 30;
+    for (const void *k : multi_kernels()) {
+        int ps = 0;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, k, kMcThreads, smem) != cudaSuccess) {
             cudaGetLastError();
             return 0;
         }
-    // both instances: the launch takes the one the tasks' flags ask for
-    int perSmHooks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, dense_sweep_multi<false>, kMcThreads, smem) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSmHooks, dense_sweep_multi<true>, kMcThreads, smem) !=
-            cudaSuccess) {
-        cudaGetLastError();
-        return 0;
+        perSm = std::min(perSm, ps);
     }
-    perSm = std::min(perSm, perSmHooks);
     cachedN = N;
     cachedCap = perSm * sms;
     return cachedCap;
@@ -1020,7 +1075,11 @@ static int launch_pack(const sq103_dense_task *tasks, int n, void *stream) {
         if (e != cudaSuccess) return (int)e;
     }
     void *args[] = {&P};
-    const void *kernel = hooks ? (const void *)dense_sweep_multi<true> : (const void *)dense_sweep_multi<false>;
+    const bool small = maxN <= kSmallN;
+    const void *kernel = small ? (hooks ? (const void *)dense_sweep_multi<true, true>
+                                        : (const void *)dense_sweep_multi<false, true>)
+                               : (hooks ? (const void *)dense_sweep_multi<true, false>
+                                        : (const void *)dense_sweep_multi<false, false>);
     return (int)cudaLaunchCooperativeKernel(kernel, dim3(ctas), dim3(kMcThreads), args, multi_smem_bytes(maxN), st);
 }
 
