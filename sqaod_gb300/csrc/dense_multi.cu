@@ -85,7 +85,7 @@ constexpr unsigned long long kShortWaitNs = 1000000ull;  // task flag kFlagShort
 // SM's shared load/store path to the decider
 constexpr int kPrefetchSleepNs = 128;
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int kSmallN = 512;  // rows up to this many spins take the kSmall instance
+constexpr int kSmallN = 448;  // rows up to this many spins take the kSmall instance (measured crossover: 384 faster, 512 slower)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
     unsigned long long v;
