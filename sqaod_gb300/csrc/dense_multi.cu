@@ -85,7 +85,7 @@ constexpr unsigned long long kShortWaitNs = 1000000ull;  // task flag kFlagShort
 // SM's shared load/store path to the decider
 constexpr int kPrefetchSleepNs = 128;
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int kSmallN = 448;  // rows up to this many spins take the kSmall instance (measured crossover: 384 faster, 512 slower)
+constexpr int kSmallN = 1024;  // rows up to this many spins take the kSmall instance (measured: 1024 faster, 2048 slower)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
     unsigned long long v;
@@ -225,11 +225,12 @@ struct McPack {
 // kHooks: the test hooks of the task flags are compiled in (short waits, a
 // trotter that withholds its accept words); the production instance has none.
 // kSmall: rows of at most kSmallN spins, where the neighbours' sites hit a lane's
-// site often: each prefetcher finds a lane's neighbour candidates by scanning the
-// 96 iterations of batches p - 2 .. p, with the sites of p - 1 and p - 2 drawn
-// again from the neighbours' Philox streams, instead of a ballot per hit over
-// the hashed-site bitmaps of the other prefetcher's batches (which makes the
-// prefetchers wait for each other).  Both give the same candidates.
+// site often: each prefetcher finds a lane's neighbour candidates from a table
+// of the positions at each site of batches p - 2 .. p (one per batch and
+// neighbour, in shared memory, cleared after use), with the sites of p - 1 and
+// p - 2 drawn again from the neighbours' Philox streams, instead of a ballot per
+// hit over the hashed-site bitmaps of the other prefetcher's batches (which
+// makes the prefetchers wait for each other).  Both give the same candidates.
 template <bool kHooks, bool kSmall>
 __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack P) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -296,7 +297,11 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
     unsigned *prePred = reinterpret_cast<unsigned *>(cand + kPre * 2 * kCand * 32);  // kPre
     int2 *flips = reinterpret_cast<int2 *>(prePred + kPre);             // 32
     int8_t *qs = reinterpret_cast<int8_t *>(flips + 32);                // N
+    // kSmall: one site table of kSmallN words per prefetcher (positions of a batch by site)
+    uint32_t *siteTab = reinterpret_cast<uint32_t *>(qs + ((N + 15) & ~15));
 
+    if (kSmall)
+        for (int i = tid; i < kPf * kSmallN; i += kMcThreads) siteTab[i] = 0u;
     for (int i = tid; i < N; i += kMcThreads) {
         Fs[i] = T.F[(size_t)y * N + i];
         hs[i] = T.h[i];
@@ -821,6 +826,9 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                             sites[nn][q] = sq;
                         }
                     }
+                    // per batch and neighbour: the positions of each site in a table
+                    // (cleared again after use), read at the lane's own site
+                    uint32_t *tab = siteTab + pw * kSmallN;
 #pragma unroll
                     for (int nn = 0; nn < 2; ++nn) {
                         if (nn >= nNbr) break;
@@ -829,16 +837,23 @@ __global__ void __launch_bounds__(kMcThreads, 2) dense_sweep_multi(const McPack 
                         // latest first: batch p, then p - 1, then p - 2, each from its last iteration
 #pragma unroll
                         for (int q = 0; q < 3; ++q) {
-                            for (int t = 31; t >= 0; --t) {
-                                const int st = __shfl_sync(FULL, sites[nn][q], t);
-                                if (valid && st == x && (q > 0 || t <= lim)) {
-                                    ++cnt;
-                                    const int jj = 32 * (p - q) + t;
-                                    if (c0 < 0)
-                                        c0 = jj;
-                                    else if (c1 < 0)
-                                        c1 = jj;
-                                }
+                            const int sq = sites[nn][q];
+                            if (sq >= 0) atomicOr(&tab[sq], 1u << lane);
+                            __syncwarp();
+                            unsigned mk = valid ? tab[x] : 0u;
+                            __syncwarp();
+                            if (sq >= 0) tab[sq] = 0u;
+                            __syncwarp();
+                            if (q == 0) mk &= lim < 0 ? 0u : (lim >= 31 ? ~0u : (2u << lim) - 1u);
+                            cnt += __popc(mk);
+                            while (mk) {
+                                const int t = 31 - __clz(mk);
+                                mk &= ~(1u << t);
+                                const int jj = 32 * (p - q) + t;
+                                if (c0 < 0)
+                                    c0 = jj;
+                                else if (c1 < 0)
+                                    c1 = jj;
                             }
                         }
                         if (cnt > kCand) c0 = -2;
@@ -986,7 +1001,7 @@ static size_t multi_smem_bytes(int N) {
     size_t ghostStride = (size_t)((N + 31) / 32 + 1) & ~(size_t)1;
     return (size_t)N * 4 * 2 + (size_t)kPre * (kJgStride + 32 + 96 + 32 + 32) * 4 + 2 * ghostStride * 4 +
            (size_t)2 * kBmSlots * kBmWords * 4 + 2 * kRing * 4 + 2 * kLogWords * 4 + (size_t)kPre * 2 * kCand * 32 * 4 + kPre * 4 +
-           32 * 8 + (size_t)N + 16;
+           32 * 8 + (size_t)((N + 15) & ~15) + 16 + (N <= kSmallN ? (size_t)kPf * kSmallN * 4 : 0);
 }
 
 static std::array<const void *, 4> multi_kernels() {
