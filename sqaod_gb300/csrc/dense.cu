@@ -36,19 +36,21 @@ struct Flip {
 
 constexpr int kBlockThreads = 512;
 
-// Applies the flips of one phase: F[y_f][i] += d_f * J[x_f][i].
-__device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F, const float *J, int ldJ, int N) {
-    int tid = threadIdx.x;
-    if (N >= kBlockThreads || nf == 1) {
+// Applies the flips of one phase, F[y_f][i] += d_f * J[x_f][i], with the nthr
+// threads t = 0 .. nthr-1.  The flips of a phase touch distinct rows, and each
+// element takes them in list order, so the result does not depend on nthr.
+__device__ __forceinline__ void apply_flips(const Flip *flips, int nf, float *F, const float *J, int ldJ, int N, int t,
+                                            int nthr) {
+    if (N >= nthr || nf == 1) {
         for (int f = 0; f < nf; ++f) {
             Flip fl = flips[f];
             float *Fy = F + (size_t)fl.y * N;
             const float *Jx = J + (size_t)fl.x * ldJ;
-            for (int i = tid; i < N; i += kBlockThreads) Fy[i] = __fmaf_rn(fl.d, __ldg(Jx + i), Fy[i]);
+            for (int i = t; i < N; i += nthr) Fy[i] = __fmaf_rn(fl.d, __ldg(Jx + i), Fy[i]);
         }
     } else {
-        int groups = kBlockThreads / N;
-        int g = tid / N, i = tid - g * N;
+        int groups = nthr / N;
+        int g = t / N, i = t - g * N;
         if (g < groups)
             for (int f = g; f < nf; f += groups) {
                 Flip fl = flips[f];
@@ -69,9 +71,63 @@ __device__ __forceinline__ int exact_dense_accept(const sq103_dense_task &T, boo
 }
 
 // Dynamic shared memory every launch of anneal_instance needs: the flip lists
-// of two phases (2 m entries) and their counters, rounded to 16 bytes.
+// of three phases (3 m entries) and their counters, rounded to 16 bytes.
 __host__ __device__ constexpr size_t flip_list_bytes(int m) {
-    return ((size_t)(2 * m) * sizeof(Flip) + 2 * sizeof(int) + 15) & ~(size_t)15;
+    return ((size_t)(3 * m) * sizeof(Flip) + 3 * sizeof(int) + 15) & ~(size_t)15;
+}
+
+// The trials of one phase: trotters yb, yb + ys, ... (cnt of them) at spin
+// index k, taken by the nthr threads t = 0 .. nthr-1.  Accepted trials flip
+// their spin, append (y, x, -2 q) to fl (counter *nfl) and set their trace bit.
+// Trials of one phase are independent: the field row of trotter y holds every
+// earlier flip of y, so its exact field is the one the trial sees.
+__device__ __forceinline__ void decide_phase(const sq103_dense_task &T, bool sa, uint32_t tag, const StepConst &sc,
+                                             const DecisionTol &tol, float G, float beta, uint32_t step, int k,
+                                             int yb, int ys, int cnt, const float *F, int8_t *q, const float *h,
+                                             Flip *fl, int *nfl, uint32_t *trace, int t0, int nthr) {
+    const int N = T.N, m = T.m;
+    for (int t = t0; t < cnt; t += nthr) {
+        int y = yb + t * ys;
+        u32x4 r = draw(T.seed, (uint32_t)k, (uint32_t)y, step, tag);
+        int x = draw_index(r.x, N);
+        float u = draw_unit(r.y);
+        size_t o = (size_t)y * N + x;
+        float qyx = q[o];
+        float dE, qL = 0.f, qR = 0.f;
+        if (sa) {
+            dE = dense_sa_dE(qyx, h[x], F[o]);
+        } else {
+            int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
+            qL = q[(size_t)yl * N + x];
+            qR = q[(size_t)yr * N + x];
+            dE = dense_sqa_dE(qyx, h[x], F[o], qL, qR, sc.twoDivM, sc.coef);
+        }
+        int nearT = 0;
+        const float L = neg_log_unit(u);
+        int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[x], __fmul_rn(2.f, F[o]), L), nearT);
+        if (nearT) acc = exact_dense_accept(T, sa, x, qyx, q + (size_t)y * N, qL, qR, G, beta, u);
+        if (acc) {
+            q[o] = (int8_t)(-qyx);
+            int slot = atomicAdd(nfl, 1);
+            fl[slot] = Flip{y, x, -2.f * qyx};
+            if (trace) {
+                uint32_t bit = (uint32_t)k * (uint32_t)m + (uint32_t)y;
+                atomicOr(&trace[bit >> 5], 1u << (bit & 31));
+            }
+        }
+    }
+}
+
+// Trotters of colour phase ph (0: even y < 2 (m/2); 1: y = m - 1 when m is odd;
+// 2: odd y) of the coloring sweep; cnt = 0 for an empty phase.
+__device__ __forceinline__ void color_phase(int m, int ph, int &yb, int &ys, int &cnt) {
+    if (ph == 0) {
+        yb = 0; ys = 2; cnt = m / 2;
+    } else if (ph == 1) {
+        yb = m - 1; ys = 1; cnt = m & 1;
+    } else {
+        yb = 1; ys = 2; cnt = m / 2;
+    }
 }
 
 // One CTA anneals one instance (all trotters) for steps [s0, s0 + nSteps) of
@@ -85,8 +141,8 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
         if (tid == 0 && T.status) atomicExch(T.status, kErrCapacity);
         return false;
     }
-    Flip *flips = reinterpret_cast<Flip *>(smem);            // 2 x m
-    int *nflip = reinterpret_cast<int *>(flips + 2 * m);      // 2 counters
+    Flip *flips = reinterpret_cast<Flip *>(smem);            // 3 x m
+    int *nflip = reinterpret_cast<int *>(flips + 3 * m);      // 3 counters
     size_t stageBytes = (size_t)m * N * 4 + (size_t)N * 4 + (size_t)m * N;
     const bool stage = off + stageBytes <= (size_t)smemBytes;
     float *F;
@@ -107,19 +163,73 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
         h = T.h;
         q = T.q;
     }
-    if (tid < 2) nflip[tid] = 0;
+    if (tid < 3) nflip[tid] = 0;
     __syncthreads();
 
     const uint32_t wordsPerStep = (uint32_t)(((size_t)N * m + 31) / 32);
+    const bool pipelined = T.algo == kColoring && m >= 2;
+    const int decideThreads = m > 64 ? 64 : 32;
+    const int accTid = pipelined ? decideThreads : 0;  // the one thread that counts accepted flips
     unsigned long long accepted = 0;
-    // flip-list buffer of the next phase; its counter is zero at the start of every
-    // phase (the one of the other buffer is cleared after each phase), so the
-    // alternation continues across steps
-    int buf = 0;
+    int buf = 0;  // flip list of the next phase (sequential order)
     __shared__ Flip naiveFlip;
     __shared__ int naiveAcc;
 
-    for (int s = s0; s < s0 + nSteps; ++s) {
+    if (pipelined) {
+        // Coloring with at least two trotters: consecutive phases hold disjoint
+        // trotter rows, and a phase reads only its own field rows and its
+        // neighbours' spins.  So the first decideThreads threads take the trials
+        // of phase p while the others apply the flips of phase p - 1; one barrier
+        // per phase.  A phase's rows were last updated two or more phases back,
+        // before a barrier.  Flip lists rotate over three buffers: the one being
+        // filled, the one being applied, and the next one, whose counter is
+        // cleared meanwhile.  Each field row still takes its trotter's flips in
+        // trial order, so fields are bit-identical to the sequential order.
+        int bc = 0;            // list of the phase being decided
+        bool pending = false;  // the previous phase's list waits to be applied
+        const int applyThreads = kBlockThreads - decideThreads;
+        for (int s = s0; s <= s0 + nSteps; ++s) {
+            const bool last = s == s0 + nSteps;  // one more stage applies the final phase
+            float G = 0.f, beta = 0.f;
+            if (!last) {
+                G = T.G ? T.G[s] : T.Gs;
+                beta = T.beta ? T.beta[s] : T.betas;
+            }
+            const StepConst sc = step_const(T.algo, m, G, beta);
+            const DecisionTol tol = decision_tol(false, true, sc.twoDivM, sc.coef, sc.rate);
+            const uint32_t step = T.step0 + (uint32_t)s;
+            uint32_t *trace = T.trace && !last ? T.trace + (size_t)(s - s0) * wordsPerStep : nullptr;
+            for (int k = 0; k < (last ? 1 : N); ++k) {
+                for (int ph = 0; ph < 3; ++ph) {
+                    int yb = 0, ys = 1, cnt = 0;
+                    if (!last) {
+                        color_phase(m, ph, yb, ys, cnt);
+                        if (cnt == 0) continue;
+                    } else if (ph) {
+                        break;
+                    }
+                    const int bp = bc == 0 ? 2 : bc - 1, bn = bc == 2 ? 0 : bc + 1;
+                    if (tid < decideThreads) {
+                        if (!last)
+                            decide_phase(T, false, kTagDenseSweep, sc, tol, G, beta, step, k, yb, ys, cnt, F, q, h,
+                                         flips + bc * m, nflip + bc, trace, tid, decideThreads);
+                    } else {
+                        if (pending) {
+                            const int nf = nflip[bp];
+                            apply_flips(flips + bp * m, nf, F, T.J, T.ldJ, N, tid - decideThreads, applyThreads);
+                            if (tid == accTid) accepted += (unsigned long long)nf;
+                        }
+                        if (tid == accTid) nflip[bn] = 0;
+                    }
+                    __syncthreads();
+                    pending = !last;
+                    bc = bn;
+                }
+            }
+        }
+    }
+
+    for (int s = s0; s < s0 + nSteps && !pipelined; ++s) {
         const float G = T.G ? T.G[s] : T.Gs, beta = T.beta ? T.beta[s] : T.betas;
         const StepConst sc = step_const(T.algo, m, G, beta);
         const DecisionTol tol = decision_tol(T.algo == kSANaive, true, sc.twoDivM, sc.coef, sc.rate);
@@ -151,12 +261,16 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
                     naiveAcc = acc;
                 }
                 __syncthreads();
-                if (naiveAcc) apply_flips(&naiveFlip, 1, F, T.J, T.ldJ, N);
+                if (naiveAcc) apply_flips(&naiveFlip, 1, F, T.J, T.ldJ, N, tid, kBlockThreads);
                 __syncthreads();
             }
             continue;
         }
 
+        // sa_naive, and coloring with one trotter: each phase's trials need the
+        // previous phase's flips applied to the same rows.
+        // Two flip lists alternate; the idle one's counter is cleared while the
+        // other is applied, so it is zero when the next phase appends to it.
         const bool sa = (T.algo == kSANaive);
         const uint32_t tag = sa ? kTagDenseSA : kTagDenseSweep;
         for (int k = 0; k < N; ++k) {
@@ -165,50 +279,16 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
                 if (sa) {
                     if (ph) break;
                     yb = 0; ys = 1; cnt = m;
-                } else if (ph == 0) {
-                    yb = 0; ys = 2; cnt = m / 2;
-                } else if (ph == 1) {
-                    if (!(m & 1)) continue;
-                    yb = m - 1; ys = 1; cnt = 1;
                 } else {
-                    yb = 1; ys = 2; cnt = m / 2;
+                    color_phase(m, ph, yb, ys, cnt);
+                    if (cnt == 0) continue;
                 }
                 Flip *fl = flips + buf * m;
-                for (int t = tid; t < cnt; t += kBlockThreads) {
-                    int y = yb + t * ys;
-                    u32x4 r = draw(T.seed, (uint32_t)k, (uint32_t)y, step, tag);
-                    int x = draw_index(r.x, N);
-                    float u = draw_unit(r.y);
-                    size_t o = (size_t)y * N + x;
-                    float qyx = q[o];
-                    float dE, qL = 0.f, qR = 0.f;
-                    if (sa) {
-                        dE = dense_sa_dE(qyx, h[x], F[o]);
-                    } else {
-                        int yl = y == 0 ? m - 1 : y - 1, yr = y == m - 1 ? 0 : y + 1;
-                        qL = q[(size_t)yl * N + x];
-                        qR = q[(size_t)yr * N + x];
-                        dE = dense_sqa_dE(qyx, h[x], F[o], qL, qR, sc.twoDivM, sc.coef);
-                    }
-                    // trials of one phase are independent: the row of trotter y holds every
-                    // earlier flip of y, so its exact field is the one this trial sees
-                    int nearT = 0;
-                    const float L = neg_log_unit(u);
-                    int acc = metropolis_log(dE, sc.rate, L, trial_xtol(tol, h[x], __fmul_rn(2.f, F[o]), L), nearT);
-                    if (nearT) acc = exact_dense_accept(T, sa, x, qyx, q + (size_t)y * N, qL, qR, G, beta, u);
-                    if (acc) {
-                        q[o] = (int8_t)(-qyx);
-                        int slot = atomicAdd(&nflip[buf], 1);
-                        fl[slot] = Flip{y, x, -2.f * qyx};
-                        if (trace) {
-                            uint32_t bit = (uint32_t)k * (uint32_t)m + (uint32_t)y;
-                            atomicOr(&trace[bit >> 5], 1u << (bit & 31));
-                        }
-                    }
-                }
+                decide_phase(T, sa, tag, sc, tol, G, beta, step, k, yb, ys, cnt, F, q, h, fl, nflip + buf, trace,
+                             tid, kBlockThreads);
                 __syncthreads();
-                int nf = nflip[buf];
-                apply_flips(fl, nf, F, T.J, T.ldJ, N);
+                const int nf = nflip[buf];
+                apply_flips(fl, nf, F, T.J, T.ldJ, N, tid, kBlockThreads);
                 if (tid == 0) {
                     nflip[buf ^ 1] = 0;
                     accepted += (unsigned long long)nf;
@@ -219,7 +299,7 @@ __device__ bool anneal_instance(const sq103_dense_task &T, unsigned char *smem, 
         }
     }
 
-    if (tid == 0 && T.accepted) atomicAdd(T.accepted, accepted);
+    if (tid == accTid && T.accepted) atomicAdd(T.accepted, accepted);
     if (stage) {
         for (size_t i = tid; i < (size_t)m * N; i += kBlockThreads) {
             T.F[i] = F[i];
