@@ -149,6 +149,20 @@ SQ103_API int sq103_dense_hamiltonian(const float *W, int ldW, int N, int maximi
 /* F = q J for all trotters (the local-field refresh). */
 SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q, float *F, int N, int m,
                                         void *stream);
+/* One instance of a batched field refresh. */
+typedef struct sq103_field_job {
+    const float *J;   /* N x N couplings, row stride ldJ */
+    const int8_t *q;  /* m x N spins */
+    float *F;         /* m x N fields */
+    int N, m, ldJ;
+    int tile0;        /* its first output tile: the sum over earlier jobs of ceil(N/64) ceil(m/64) */
+} sq103_field_job;
+/* F = q J of every job in one launch (no counterpart in the reference: the batch
+ * refreshes its many small instances together).  jobs and tileJob (the job of
+ * each of the nTiles output tiles, in tile order) in device memory.  Each job's
+ * fields are bit-identical to sq103_dense_field_refresh of that job. */
+SQ103_API int sq103_dense_field_refresh_batch(const sq103_field_job *jobs, const int *tileJob, int nTiles,
+                                              void *stream);
 /* FP64 Ising energies of all trotters (calculate_E; sqaodc/cuda/DeviceFormulas.cpp:42-49);
  * the row sums q J are accumulated in double-float (about 2^-44 relative).
  * r_scratch: m x N doubles. */

@@ -28,14 +28,15 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
     c = __fadd_rn(c, err);
 }
 
-// EXACT = false: fp32 fields; true: double-float energy row sums (OutT double)
+// The 64 x 64 output tile at rows y0.., columns n0.. of C = A B, by a CTA of 256
+// threads.  EXACT = false: fp32 fields; true: double-float energy row sums (OutT
+// double).
 template <bool EXACT, typename OutT>
-__global__ void __launch_bounds__(256) field_gemm_kernel(const int8_t *A, int lda, const float *B, int ldb, OutT *C,
-                                                         int ldc, int M, int Nn, int K) {
+__device__ __forceinline__ void field_gemm_tile(const int8_t *A, int lda, const float *B, int ldb, OutT *C, int ldc,
+                                                int M, int Nn, int K, int y0, int n0) {
     __shared__ __align__(16) float As[2][32][68];  // rows padded against store conflicts
     __shared__ __align__(16) float Bs[2][32][68];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int y0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
     // loader roles: A row ar, k ak..ak+7; B row bk, columns bc..bc+3 and bc+32..bc+35
     const int ar = tid >> 2, ak = (tid & 3) * 8;
     const int bk = tid >> 3, bc = (tid & 7) * 4;
@@ -149,6 +150,12 @@ __global__ void __launch_bounds__(256) field_gemm_kernel(const int8_t *A, int ld
                 C[(size_t)y * ldc + n] = (OutT)__fadd_rn(s[a][b], c[a][b]);
         }
     }
+}
+
+template <bool EXACT, typename OutT>
+__global__ void __launch_bounds__(256) field_gemm_kernel(const int8_t *A, int lda, const float *B, int ldb, OutT *C,
+                                                         int ldc, int M, int Nn, int K) {
+    field_gemm_tile<EXACT, OutT>(A, lda, B, ldb, C, ldc, M, Nn, K, blockIdx.y * 64, blockIdx.x * 64);
 }
 
 }  // namespace sq103

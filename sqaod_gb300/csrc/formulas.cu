@@ -180,6 +180,15 @@ __global__ void __launch_bounds__(256) ring_dot(const int8_t *q, int N, int m, l
     if (threadIdx.x == 0) atomicAdd((unsigned long long *)out, (unsigned long long)(long long)t);
 }
 
+// One 64 x 64 tile of one job's fields per CTA; the tile arithmetic is the one
+// of field_gemm_kernel, so each job's fields equal its own refresh bit for bit.
+__global__ void __launch_bounds__(256) field_gemm_batch_kernel(const sq103_field_job *jobs, const int *tileJob) {
+    const sq103_field_job jb = jobs[tileJob[blockIdx.x]];
+    const int local = (int)blockIdx.x - jb.tile0, tilesN = (jb.N + 63) / 64;
+    const int ty = local / tilesN, tx = local - ty * tilesN;
+    field_gemm_tile<false, float>(jb.q, jb.N, jb.J, jb.ldJ, jb.F, jb.N, jb.m, jb.N, jb.N, ty * 64, tx * 64);
+}
+
 }  // namespace sq103
 
 using namespace sq103;
@@ -213,6 +222,14 @@ SQ103_API int sq103_dense_field_refresh(const float *J, int ldJ, const int8_t *q
     cudaStream_t s = (cudaStream_t)stream;
     dim3 grid((N + 63) / 64, (m + 63) / 64);
     field_gemm_kernel<false, float><<<grid, 256, 0, s>>>(q, N, J, ldJ, F, N, m, N, N);
+    return (int)cudaGetLastError();
+}
+
+SQ103_API int sq103_dense_field_refresh_batch(const sq103_field_job *jobs, const int *tileJob, int nTiles,
+                                              void *stream) {
+    if (nTiles < 0 || (nTiles > 0 && (!jobs || !tileJob))) return kErrBadShape;
+    if (nTiles == 0) return 0;
+    field_gemm_batch_kernel<<<nTiles, 256, 0, (cudaStream_t)stream>>>(jobs, tileJob);
     return (int)cudaGetLastError();
 }
 

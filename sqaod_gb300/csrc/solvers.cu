@@ -1951,7 +1951,6 @@ public:
         for (int i = 0; i < nAll; ++i) {
             Inst &in = *insts_[i];
             SQ_CHECK(sq103_randomize_spins(in.q, in.N, in.m, in.seed, 0, 0, st_.get()));
-            refresh(in);
             in.multi = multiMinN_ > 0 && in.N >= multiMinN_ && in.m >= 2 && sq103_dense_multicta_ok(in.N, in.m, kColoring);
             if (in.multi) {
                 in.wsBytes = sq103_dense_ws_bytes(in.N, in.m, kRefreshPeriod);
@@ -1979,6 +1978,8 @@ public:
             maxN = std::max(maxN, in.N);
             maxM = std::max(maxM, in.m);
         }
+        buildRefreshJobs();
+        refreshAll();
         // packed launches take instances of similar size together
         std::stable_sort(multi_.begin(), multi_.end(), [](const Inst *a, const Inst *b) { return a->N < b->N; });
         // largest instances first: the queue then balances the tail
@@ -2223,8 +2224,45 @@ private:
         flush();
     }
 
+    // Instances below the tensor-core refresh size take the SIMT refresh, all of
+    // them in one launch (one CTA per 64 x 64 tile of any instance's fields);
+    // the others refresh on the tensor cores one by one.
+    void buildRefreshJobs() {
+        std::vector<sq103_field_job> jobs;
+        std::vector<int> tileJob;
+        tcInsts_.clear();
+        for (auto &p : insts_) {
+            Inst &in = *p;
+            if (in.digits.p) {
+                tcInsts_.push_back(&in);
+                continue;
+            }
+            sq103_field_job j = {};
+            j.J = in.J;
+            j.q = in.q;
+            j.F = in.F;
+            j.N = in.N;
+            j.m = in.m;
+            j.ldJ = in.ldJ;
+            j.tile0 = (int)tileJob.size();
+            const int tiles = ((in.N + 63) / 64) * ((in.m + 63) / 64);
+            tileJob.insert(tileJob.end(), tiles, (int)jobs.size());
+            jobs.push_back(j);
+        }
+        nTiles_ = (int)tileJob.size();
+        if (jobs.empty()) return;
+        dJobs_.ensure(jobs.size());
+        dTileJob_.ensure(tileJob.size());
+        SQ_CHECK(cudaMemcpyAsync(dJobs_.p, jobs.data(), sizeof(sq103_field_job) * jobs.size(), cudaMemcpyHostToDevice,
+                                 st_.get()));
+        SQ_CHECK(cudaMemcpyAsync(dTileJob_.p, tileJob.data(), sizeof(int) * tileJob.size(), cudaMemcpyHostToDevice,
+                                 st_.get()));
+        st_.sync();
+    }
+
     void refreshAll() {
-        for (auto &p : insts_) refresh(*p);
+        for (Inst *in : tcInsts_) refresh(*in);
+        SQ_CHECK(sq103_dense_field_refresh_batch(dJobs_.p, dTileJob_.p, nTiles_, st_.get()));
     }
 
     void captureStep() {
@@ -2243,6 +2281,10 @@ private:
     DevBuf<double> scratch_, r_, E64_;
     DevBuf<sq103_dense_task> dTasks_;
     DevBuf<int> dOrder_, dPos_, dQueue_, dStatus_;
+    DevBuf<sq103_field_job> dJobs_;  // the SIMT refresh of every instance below the tensor-core size
+    DevBuf<int> dTileJob_;
+    int nTiles_ = 0;
+    std::vector<Inst *> tcInsts_;     // instances refreshed on the tensor cores
     std::vector<Inst *> multi_;  // the instances on the one-CTA-per-trotter sweep, by N
     cudaGraphExec_t graph_ = nullptr;
     int nSched_ = 0, pos_ = 0, grid_ = 1, smem_ = -1, nSmall_ = 0, multiMinN_ = kDefaultMultiMinN;

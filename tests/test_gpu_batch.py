@@ -91,3 +91,50 @@ def test_batch_routing_autotune_keeps_results():
         a.anneal(G, 30.0)
         assert np.array_equal(np.array(a.get_q()), b.get_q(i)), i
         assert np.array_equal(a.get_E64(), b.get_E64(i)), i
+
+
+def test_field_refresh_batch_equals_single_refresh():
+    """sq103_dense_field_refresh_batch (one launch over every job's tiles) gives
+    each job the fields of its own sq103_dense_field_refresh, bit for bit: ragged
+    N and m, more than 64 trotters, padded rows (the padding holds NaN, so a read
+    past N would show)."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from sqaod_gb300 import _lib
+    L = _lib.lib()
+
+    class FieldJob(ctypes.Structure):
+        _fields_ = [("J", ctypes.c_void_p), ("q", ctypes.c_void_p), ("F", ctypes.c_void_p),
+                    ("N", ctypes.c_int), ("m", ctypes.c_int), ("ldJ", ctypes.c_int), ("tile0", ctypes.c_int)]
+
+    dev = torch.device("cuda", 0)
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(7)
+    shapes = [(40, 3), (64, 64), (100, 65), (130, 16), (37, 128), (1, 1), (200, 8), (513, 33)]
+    jobs, tile_job, keep, singles = [], [], [], []
+    for j, (N, m) in enumerate(shapes):
+        ldJ = (N + 3) & ~3
+        Jh = np.full((N, ldJ), np.nan, np.float32)
+        Jh[:, :N] = rng.uniform(-1, 1, (N, N)).astype(np.float32)
+        qh = rng.choice(np.array([-1, 1], np.int8), (m, N))
+        dJ = torch.from_numpy(Jh).to(dev)
+        dq = torch.from_numpy(qh).to(dev)
+        Fb = torch.full((m, N), -7.0, dtype=torch.float32, device=dev)
+        Fs = torch.empty((m, N), dtype=torch.float32, device=dev)
+        assert L.sq103_dense_field_refresh(ctypes.c_void_p(dJ.data_ptr()), ldJ, ctypes.c_void_p(dq.data_ptr()),
+                                           ctypes.c_void_p(Fs.data_ptr()), N, m, sp) == 0
+        jobs.append(FieldJob(dJ.data_ptr(), dq.data_ptr(), Fb.data_ptr(), N, m, ldJ, len(tile_job)))
+        tile_job += [j] * (((N + 63) // 64) * ((m + 63) // 64))
+        keep += [dJ, dq]
+        singles.append((Fs, Fb))
+    arr = (FieldJob * len(jobs))(*jobs)
+    dJobs = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev)
+    dTiles = torch.tensor(tile_job, dtype=torch.int32, device=dev)
+    assert L.sq103_dense_field_refresh_batch(ctypes.c_void_p(dJobs.data_ptr()), ctypes.c_void_p(dTiles.data_ptr()),
+                                             len(tile_job), sp) == 0
+    torch.cuda.synchronize()
+    for (N, m), (Fs, Fb) in zip(shapes, singles):
+        assert torch.equal(Fs.view(torch.int32), Fb.view(torch.int32)), (N, m)
+        assert torch.isfinite(Fb).all(), (N, m)
+    assert L.sq103_dense_field_refresh_batch(None, None, 0, sp) == 0
+    assert L.sq103_dense_field_refresh_batch(None, None, 3, sp) != 0
