@@ -260,15 +260,39 @@ public:
             SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
         }
         std::vector<Request *> finished;
+        jobs_.clear();
+        tileJob_.clear();
         for (auto &kv : active_) {
             Request *r = kv.second;
             if (r->kind == kSearch) continue;   // advanced below
             if (r->pos >= r->nSteps) continue;  // finishing: its results are being collected
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
-            if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0)
-                SQ_CHECK(sq103_dense_refresh(r->dt.J, r->dt.ldJ, r->digits, r->spinsBf16, r->dt.q, r->dt.F, r->N0,
-                                             r->m, r->dStatus, st_.get()));
+            if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0) {
+                if (r->digits) {
+                    SQ_CHECK(sq103_dense_refresh(r->dt.J, r->dt.ldJ, r->digits, r->spinsBf16, r->dt.q, r->dt.F, r->N0,
+                                                 r->m, r->dStatus, st_.get()));
+                } else {  // below the tensor-core size: with the others, in one launch
+                    sq103_field_job j = {};
+                    j.J = r->dt.J;
+                    j.q = r->dt.q;
+                    j.F = r->dt.F;
+                    j.N = r->N0;
+                    j.m = r->m;
+                    j.ldJ = r->dt.ldJ;
+                    j.tile0 = (int)tileJob_.size();
+                    tileJob_.insert(tileJob_.end(), ((r->N0 + 63) / 64) * ((r->m + 63) / 64), (int)jobs_.size());
+                    jobs_.push_back(j);
+                }
+            }
             if (r->pos >= r->nSteps) finished.push_back(r);
+        }
+        if (!jobs_.empty()) {
+            // grown rarely (a larger buffer frees the old one, which waits for the device)
+            dJobs_.ensure(std::max<size_t>(jobs_.size(), 1024));
+            dTileJob_.ensure(std::max<size_t>(tileJob_.size(), 16384));
+            stage_.copy(dJobs_.p, jobs_.data(), sizeof(sq103_field_job) * jobs_.size(), st_.get());
+            stage_.copy(dTileJob_.p, tileJob_.data(), sizeof(int) * tileJob_.size(), st_.get());
+            SQ_CHECK(sq103_dense_field_refresh_batch(dJobs_.p, dTileJob_.p, (int)tileJob_.size(), st_.get()));
         }
         for (Request *r : finished) finish(r);
         // searches: the next range of each, on the searcher's stream (the anneals
@@ -396,7 +420,7 @@ private:
     }
 
     bool fitsStaging(const Request &r) const {
-        size_t base = ((size_t)(2 * r.m) * 12 + 8 + 15) & ~(size_t)15;
+        const size_t base = (size_t)sq103_dense_batch_min_smem(r.m);  // the flip lists
         return base + (size_t)r.m * r.N0 * 5 + (size_t)r.N0 * 4 <= (size_t)stageSmem_;
     }
 
@@ -685,6 +709,11 @@ private:
     }
 
     Stream st_, res_;  // work; result copies
+    // this tick's SIMT field refreshes (host table, device copy)
+    std::vector<sq103_field_job> jobs_;
+    std::vector<int> tileJob_;
+    DevBuf<sq103_field_job> dJobs_;
+    DevBuf<int> dTileJob_;
     PinnedStage stage_;
     unsigned long long budget_, used_ = 0;
     int maxSlots_, maxLarge_ = 64, sms_ = 0, denseGrid_ = 1, bipGrid_ = 1, stageSmem_ = 0, nextId_ = 0, done_ = 0;
