@@ -1888,6 +1888,9 @@ public:
 
     ~DenseBatch() {
         if (graph_) cudaGraphExecDestroy(graph_);
+        if (fork_) cudaEventDestroy(fork_);
+        for (cudaEvent_t e : join_)
+            if (e) cudaEventDestroy(e);
     }
 
     int add(const float *W, int N, int m, int optimize, unsigned long long seed) {
@@ -2260,9 +2263,28 @@ private:
         st_.sync();
     }
 
+    // The tensor-core refreshes are independent and each fills only part of the
+    // GPU: they run on kRefreshStreams side streams, forked from and joined back
+    // into the batch's stream with events (the same kernels, so the same fields).
     void refreshAll() {
-        for (Inst *in : tcInsts_) refresh(*in);
         SQ_CHECK(sq103_dense_field_refresh_batch(dJobs_.p, dTileJob_.p, nTiles_, st_.get()));
+        if (tcInsts_.empty()) return;
+        const int ns = (int)std::min<size_t>(kRefreshStreams, tcInsts_.size());
+        if (!fork_) {
+            SQ_CHECK(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+            for (cudaEvent_t &e : join_) SQ_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+        SQ_CHECK(cudaEventRecord(fork_, st_.get()));
+        for (int k = 0; k < ns; ++k) SQ_CHECK(cudaStreamWaitEvent(side_[k].get(), fork_, 0));
+        for (size_t i = 0; i < tcInsts_.size(); ++i) {
+            Inst &in = *tcInsts_[i];
+            SQ_CHECK(sq103_dense_refresh(in.J, in.ldJ, in.digits.p, in.Abf.p, in.q, in.F, in.N, in.m, in.status,
+                                         side_[i % ns].get()));
+        }
+        for (int k = 0; k < ns; ++k) {
+            SQ_CHECK(cudaEventRecord(join_[k], side_[k].get()));
+            SQ_CHECK(cudaStreamWaitEvent(st_.get(), join_[k], 0));
+        }
     }
 
     void captureStep() {
@@ -2285,6 +2307,9 @@ private:
     DevBuf<int> dTileJob_;
     int nTiles_ = 0;
     std::vector<Inst *> tcInsts_;     // instances refreshed on the tensor cores
+    static constexpr int kRefreshStreams = 4;
+    Stream side_[kRefreshStreams];
+    cudaEvent_t fork_ = nullptr, join_[kRefreshStreams] = {};
     std::vector<Inst *> multi_;  // the instances on the one-CTA-per-trotter sweep, by N
     cudaGraphExec_t graph_ = nullptr;
     int nSched_ = 0, pos_ = 0, grid_ = 1, smem_ = -1, nSmall_ = 0, multiMinN_ = kDefaultMultiMinN;
