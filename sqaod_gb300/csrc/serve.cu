@@ -148,6 +148,8 @@ public:
         counts_.ensure(2);
         queues_.ensure(4);
         stage_.init((size_t)96 << 20);
+        SQ_CHECK(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+        for (cudaEvent_t &e : join_) SQ_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         SQ_CHECK(cudaMemsetAsync(queues_.p, 0, sizeof(int) * 4, st_.get()));
         SQ_CHECK(cudaMemsetAsync(counts_.p, 0, sizeof(int) * 2, st_.get()));
         int dev = 0;
@@ -169,6 +171,8 @@ public:
     ~Server() {
         for (Request *r : finishing_)
             if (r->done) cudaEventDestroy(r->done);
+        cudaEventDestroy(fork_);
+        for (cudaEvent_t e : join_) cudaEventDestroy(e);
     }
 
     int submitDense(const float *W, int N, int m, int optimize, unsigned long long seed, const float *G,
@@ -262,15 +266,21 @@ public:
         std::vector<Request *> finished;
         jobs_.clear();
         tileJob_.clear();
+        int nTc = 0;  // tensor-core refreshes queued on the side streams
         for (auto &kv : active_) {
             Request *r = kv.second;
             if (r->kind == kSearch) continue;   // advanced below
             if (r->pos >= r->nSteps) continue;  // finishing: its results are being collected
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0) {
-                if (r->digits) {
+                if (r->digits) {  // on the side streams, forked from the work stream at the first
+                    if (nTc == 0) {
+                        SQ_CHECK(cudaEventRecord(fork_, st_.get()));
+                        for (Stream &x : side_) SQ_CHECK(cudaStreamWaitEvent(x.get(), fork_, 0));
+                    }
                     SQ_CHECK(sq103_dense_refresh(r->dt.J, r->dt.ldJ, r->digits, r->spinsBf16, r->dt.q, r->dt.F, r->N0,
-                                                 r->m, r->dStatus, st_.get()));
+                                                 r->m, r->dStatus, side_[nTc % kRefreshStreams].get()));
+                    ++nTc;
                 } else {  // below the tensor-core size: with the others, in one launch
                     sq103_field_job j = {};
                     j.J = r->dt.J;
@@ -294,6 +304,11 @@ public:
             stage_.copy(dTileJob_.p, tileJob_.data(), sizeof(int) * tileJob_.size(), st_.get());
             SQ_CHECK(sq103_dense_field_refresh_batch(dJobs_.p, dTileJob_.p, (int)tileJob_.size(), st_.get()));
         }
+        if (nTc > 0)  // join: the next work on the stream sees every refreshed field
+            for (int k = 0; k < kRefreshStreams; ++k) {
+                SQ_CHECK(cudaEventRecord(join_[k], side_[k].get()));
+                SQ_CHECK(cudaStreamWaitEvent(st_.get(), join_[k], 0));
+            }
         for (Request *r : finished) finish(r);
         // searches: the next range of each, on the searcher's stream (the anneals
         // queued above run meanwhile)
@@ -709,6 +724,10 @@ private:
     }
 
     Stream st_, res_;  // work; result copies
+    // the tensor-core field refreshes of a tick, side by side (each fills only part of the GPU)
+    static constexpr int kRefreshStreams = 4;
+    Stream side_[kRefreshStreams];
+    cudaEvent_t fork_ = nullptr, join_[kRefreshStreams] = {};
     // this tick's SIMT field refreshes (host table, device copy)
     std::vector<sq103_field_job> jobs_;
     std::vector<int> tileJob_;
