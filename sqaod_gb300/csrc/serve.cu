@@ -254,15 +254,21 @@ public:
             packN = std::max(packN, r->N0);
         }
         flush();
+        // large bipartite requests: each one's launches in order on one of the side
+        // streams, the requests side by side (each fills only part of the GPU)
+        int nBig = 0;
         for (Request *r : large_) {
             if (r->kind != 1) continue;
+            if (nBig == 0) fork();
             sq103_bipartite_task t = r->bt;
             t.G = r->bt.G + r->pos;
             t.beta = r->bt.beta + r->pos;
             t.step0 = 1 + (uint32_t)r->pos;
             t.nSteps = std::min(kStepsPerTick, r->nSteps - r->pos);
-            SQ_CHECK(sq103_bipartite_anneal(&t, st_.get()));
+            SQ_CHECK(sq103_bipartite_anneal(&t, side_[nBig % kRefreshStreams].get()));
+            ++nBig;
         }
+        if (nBig > 0) join();
         std::vector<Request *> finished;
         jobs_.clear();
         tileJob_.clear();
@@ -274,10 +280,7 @@ public:
             r->pos = std::min(r->pos + kStepsPerTick, r->nSteps);
             if (r->kind == 0 && r->pos < r->nSteps && r->pos % kRefreshPeriod == 0) {
                 if (r->digits) {  // on the side streams, forked from the work stream at the first
-                    if (nTc == 0) {
-                        SQ_CHECK(cudaEventRecord(fork_, st_.get()));
-                        for (Stream &x : side_) SQ_CHECK(cudaStreamWaitEvent(x.get(), fork_, 0));
-                    }
+                    if (nTc == 0) fork();
                     SQ_CHECK(sq103_dense_refresh(r->dt.J, r->dt.ldJ, r->digits, r->spinsBf16, r->dt.q, r->dt.F, r->N0,
                                                  r->m, r->dStatus, side_[nTc % kRefreshStreams].get()));
                     ++nTc;
@@ -304,11 +307,7 @@ public:
             stage_.copy(dTileJob_.p, tileJob_.data(), sizeof(int) * tileJob_.size(), st_.get());
             SQ_CHECK(sq103_dense_field_refresh_batch(dJobs_.p, dTileJob_.p, (int)tileJob_.size(), st_.get()));
         }
-        if (nTc > 0)  // join: the next work on the stream sees every refreshed field
-            for (int k = 0; k < kRefreshStreams; ++k) {
-                SQ_CHECK(cudaEventRecord(join_[k], side_[k].get()));
-                SQ_CHECK(cudaStreamWaitEvent(st_.get(), join_[k], 0));
-            }
+        if (nTc > 0) join();  // the next work on the stream sees every refreshed field
         for (Request *r : finished) finish(r);
         // searches: the next range of each, on the searcher's stream (the anneals
         // queued above run meanwhile)
@@ -331,6 +330,19 @@ public:
         // collected results free): wait for the results still being computed
         if (active_.size() == finishing_.size()) return nDone + nSearched + finalizeReady(true);
         return nDone + nSearched;
+    }
+
+    // the side streams start after the work queued so far on the work stream ...
+    void fork() {
+        SQ_CHECK(cudaEventRecord(fork_, st_.get()));
+        for (Stream &x : side_) SQ_CHECK(cudaStreamWaitEvent(x.get(), fork_, 0));
+    }
+    // ... and the work stream continues after everything queued on them
+    void join() {
+        for (int k = 0; k < kRefreshStreams; ++k) {
+            SQ_CHECK(cudaEventRecord(join_[k], side_[k].get()));
+            SQ_CHECK(cudaStreamWaitEvent(st_.get(), join_[k], 0));
+        }
     }
 
     int state(int id) const {
@@ -724,7 +736,8 @@ private:
     }
 
     Stream st_, res_;  // work; result copies
-    // the tensor-core field refreshes of a tick, side by side (each fills only part of the GPU)
+    // side streams for a tick's large bipartite requests and tensor-core field
+    // refreshes, which each fill only part of the GPU
     static constexpr int kRefreshStreams = 4;
     Stream side_[kRefreshStreams];
     cudaEvent_t fork_ = nullptr, join_[kRefreshStreams] = {};

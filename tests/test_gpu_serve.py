@@ -95,6 +95,52 @@ def test_server_requests_match_alone():
             assert np.array_equal(q[1], np.array([p[1] for p in q1])), i
 
 
+def test_server_large_bipartite_requests_side_by_side():
+    """Large bipartite requests (m N0 N1 > 2^22, the per-instance kernels) of
+    different shapes and lengths step side by side on the server's side streams,
+    beside large and small dense requests whose fields refresh in the same
+    ticks; each ends bit-identical to annealing it alone."""
+    import sqaod_gb300 as sq
+    from sqaod_gb300.serve import AnnealServer
+    specs = [("b", (512, 512), 32, 17, "min"), ("b", (300, 400), 64, 9, "max"), ("b", (256, 1024), 24, 12, "min"),
+             ("b", (2048, 1024), 8, 10, "min"), ("b", (640, 200), 40, 20, "max"),
+             ("b", (2048, 2048), 256, 8, "min"),  # half-step fields on the tensor cores
+             ("d", 1500, 16, 12, "min"),
+             ("d", 1024, 8, 16, "min"), ("d", 300, 16, 11, "min"), ("d", 80, 4, 9, "max")]
+    rng = np.random.default_rng(31)
+    data = []
+    for kind, sizes, m, steps, opt in specs:
+        if kind == "d":
+            data.append(_sym(rng, sizes))
+        else:
+            N0, N1 = sizes
+            data.append((rng.uniform(-1, 1, N0).astype(np.float32), rng.uniform(-1, 1, N1).astype(np.float32),
+                         rng.uniform(-1, 1, (N1, N0)).astype(np.float32)))
+    srv = AnnealServer(budget_bytes=1 << 30, max_slots=8)
+    srv.set_large_limit(16)
+    ids = []
+    for i, (spec, d) in enumerate(zip(specs, data)):
+        kind, sizes, m, steps, opt = spec
+        G, beta = _schedule(steps)
+        o = sq.maximize if opt == "max" else sq.minimize
+        if kind == "d":
+            ids.append(srv.submit_dense(d, m, G, beta, o, seed=3100 + i))
+        else:
+            ids.append(srv.submit_bipartite(d[0], d[1], d[2], m, G, beta, o, seed=3100 + i))
+    srv.tick()
+    assert srv.stats()["active"] == len(specs)  # all admitted together
+    assert srv.run(max_ticks=100) < 100
+    for i, (spec, d, rid) in enumerate(zip(specs, data, ids)):
+        E, q = srv.result(rid)
+        E1, q1 = _alone(sq, spec, d, 3100 + i)
+        assert np.array_equal(E, E1), (i, E, E1)
+        if spec[0] == "d":
+            assert np.array_equal(q, np.array(q1)), i
+        else:
+            assert np.array_equal(q[0], np.array([p[0] for p in q1])), i
+            assert np.array_equal(q[1], np.array([p[1] for p in q1])), i
+
+
 def test_server_packs_large_dense_requests():
     """Large dense requests of different sizes and lengths step together in
     packed cooperative launches; each still ends bit-identical to annealing it alone."""
