@@ -1881,11 +1881,6 @@ public:
         int *status;
     };
 
-    void refresh(Inst &in) {
-        SQ_CHECK(sq103_dense_refresh(in.J, in.ldJ, in.digits.p, in.Abf.p, in.q, in.F, in.N, in.m, in.status,
-                                     st_.get()));
-    }
-
     ~DenseBatch() {
         if (graph_) cudaGraphExecDestroy(graph_);
         if (fork_) cudaEventDestroy(fork_);
