@@ -122,6 +122,14 @@ def test_input_checks_on_host():
         sq.cuda.bipartite_graph_annealer().set_qubo(np.zeros(3), np.zeros(4), np.zeros((3, 3)))
 
 
+def test_field_refresh_batch_argument_checks_on_host(lib):
+    """The batched field refresh checks its table before any launch: no tiles is
+    a no-op, tiles without a table or a negative count are rejected."""
+    assert lib.sq103_dense_field_refresh_batch(None, None, 0, None) == 0
+    assert lib.sq103_dense_field_refresh_batch(None, None, 5, None) != 0
+    assert lib.sq103_dense_field_refresh_batch(None, None, -1, None) != 0
+
+
 def test_symmetrize_rules():
     import sqaod_gb300 as sq
     W = np.triu(np.arange(16, dtype=np.float32).reshape(4, 4))
